@@ -1,0 +1,402 @@
+"""Benchmark of the GB300 GAS engine (one JSON line on stdout).
+
+Default workload: SSSP on the 1024x1024 4-neighbour lattice with 15% of its
+edges deleted (largest component kept, relabelled row-major), int32 weights
+uniform in [1, 100], source 0, every vertex active at start -- the
+configuration the reference's GTEPS metric is quoted on for one GPU.
+A step is one full run(): rounds of gather/apply + scatter/activate until no
+vertex is active, from the driver's initial vertex data (sssp.cu:67-82).
+
+  value   GTEPS = edges traversed (in-edges gathered + out-edges scattered,
+          summed over rounds) / device time, inputs resident in HBM
+  e2e     the same through the C ABI with host buffers: vertex data H2D
+          from pinned memory, run(), results D2H, every step
+  roofline  the dominant kernel's algorithmic bytes / its CUDA-event time
+  cpu_baseline  the oracle (CPU restatement of the reference engine) on
+          the same graph, one run on one core
+
+--impl reference times the reference's CPU engine (oracle/_ref where it
+was built, else the oracle restatement) with every host core running one
+instance of the same workload.
+
+Multi-GPU: replicas only (every rank runs the workload on its own GPU; the
+path has no exchange step); value sums the ranks' edges over the slowest
+rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
+
+WORKLOADS = {
+    "sssp-grid1024": dict(desc="SSSP, 1024x1024 lattice, 15% edges deleted, LCC, w in [1,100], source 0"),
+    "bfs-rmat16": dict(desc="BFS, R-MAT scale 16 ef 16 (0.57/0.19/0.19), symmetrised, source = max out-degree"),
+    "pagerank-rmat22": dict(desc="PageRank FP32 (0.85, tol 0.01, <=50 rounds), R-MAT scale 22 ef 16, directed"),
+    "cc-rmat22": dict(desc="connected components, R-MAT scale 22 ef 16, symmetrised"),
+}
+SEED = 1
+
+
+def make_workload(name: str):
+    from vertexapi2_gb300 import graphs
+    from vertexapi2_gb300 import programs as P
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_CC, PROGRAM_PAGERANK, PROGRAM_SSSP
+    if name == "sssp-grid1024":
+        g = graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100))
+        return dict(program=PROGRAM_SSSP, g=g, source=0, init=P.sssp_init(g.n_vertices, 0),
+                    active=(0, g.n_vertices), max_iters=0, vd_bytes=4, ed_bytes=4, gather=True)
+    if name == "bfs-rmat16":
+        g = graphs.rmat(16, 16, seed=SEED, symmetrize=True)
+        s = P.max_outdegree_vertex(g.n_vertices, g.srcs)
+        return dict(program=PROGRAM_BFS, g=g, source=s, init=P.bfs_init(g.n_vertices),
+                    active=(s, s + 1), max_iters=0, vd_bytes=4, ed_bytes=0, gather=False)
+    if name == "pagerank-rmat22":
+        g = graphs.rmat(22, 16, seed=SEED)
+        return dict(program=PROGRAM_PAGERANK, g=g, source=0, init=P.pagerank_init(g.n_vertices, g.srcs),
+                    active=(0, g.n_vertices), max_iters=50, vd_bytes=8, ed_bytes=0, gather=True)
+    if name == "cc-rmat22":
+        g = graphs.rmat(22, 16, seed=SEED, symmetrize=True)
+        return dict(program=PROGRAM_CC, g=g, source=0, init=P.cc_init(g.n_vertices),
+                    active=(0, g.n_vertices), max_iters=0, vd_bytes=4, ed_bytes=0, gather=True)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def round_bytes(st: dict, vd: int, ed: int, gather: bool):
+    """Algorithmic (compulsory) bytes per round, gather+apply and scatter.
+
+    gather+apply: |A|*(4 id + 8 offset pair + 2*VD read/write + 1 ret)
+                  + |E_in|*(4 source id + ED + VD of the source)
+    apply only:   |A|*(4 id + 2*VD + 1 ret)
+    scatter:      |R|*8 offset pair + |E_out|*4 destination id
+                  + 4 per vertex appended to the next frontier
+    """
+    a, ein, r, eout = (st[k].astype(np.float64) for k in ("active", "gathered", "ret", "scattered"))
+    if gather:
+        g = a * (4 + 8 + 2 * vd + 1) + ein * (4 + ed + vd)
+    else:
+        g = a * (4 + 2 * vd + 1)
+    nxt = np.concatenate([a[1:], [0.0]])
+    s = r * 8 + eout * 4 + nxt * 4
+    return g, s
+
+
+def measured_peak() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.path or not os.path.exists(self.path):
+            return None
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                maxs.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sms:
+            return None
+        return {"sm_mhz": float(np.median(sms)), "sm_max_mhz": float(max(maxs)),
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_run(engine, w, name):
+    g = w["g"]
+    if name == "sssp-grid1024":
+        _, st = engine.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, w["source"], stats_cap=1 << 14)
+    elif name == "bfs-rmat16":
+        _, st = engine.bfs(g.n_vertices, g.srcs, g.dsts, w["source"], stats_cap=1 << 14)
+    elif name == "pagerank-rmat22":
+        _, st = engine.pagerank(g.n_vertices, g.srcs, g.dsts, max_iters=50, stats_cap=1 << 14)
+    else:
+        _, st = engine.cc(g.n_vertices, g.srcs, g.dsts, stats_cap=1 << 14)
+    return st
+
+
+def run_reference(args):
+    """CPU reference engine on every host core (rank 0 only)."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    import oracle
+    eng = oracle.ref() or oracle.port()
+    w = make_workload(args.workload)
+    port = oracle.port()
+    # traversed edges per run (from the restatement's instrumented counts)
+    st = cpu_run(port, w, args.workload)
+    edges = float(st["gathered"].sum() + st["scattered"].sum())
+    cores = os.cpu_count() or 1
+
+    def one_step():
+        ts = [threading.Thread(target=cpu_run, args=(eng, w, args.workload)) for _ in range(cores)]
+        t0 = time.perf_counter()
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one_step()
+    times = [one_step() for _ in range(args.steps)]
+    total = sum(times)
+    value = cores * edges * args.steps / total / 1e9
+    line = {
+        "impl": "reference", "metric": "GTEPS & %HBM roofline per algo", "value": value,
+        "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                   "n_vertices": w["g"].n_vertices, "n_edges": w["g"].n_edges, "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": eng.kind,
+                         "sample": f"{cores} concurrent full runs of the workload per step"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    import vertexapi2_gb300 as gas
+    gas.load()
+    if not gas.device_supported(local):
+        raise SystemExit(f"cuda:{local} is not an sm_103 device")
+    w = make_workload(args.workload)
+    g = w["g"]
+    stream = torch.cuda.current_stream()
+    eng = gas.GASEngine(w["program"], device=local, stream=stream.cuda_stream)
+    init = w["init"].copy()
+    ed = g.weights if w["ed_bytes"] else None
+    eng.set_graph(g.n_vertices, init, g.srcs, g.dsts, ed)
+    eng.save_vertex_data()
+    lo, hi = w["active"]
+
+    def device_step():
+        eng.restore_vertex_data()
+        eng.set_active(lo, hi)
+        return eng.run(w["max_iters"])
+
+    for _ in range(max(args.warmup, 1)):
+        rounds = device_step()
+    stats = eng.round_stats()
+    edges_per_run = float(stats["gathered"].sum() + stats["scattered"].sum())
+    # per-kernel CUDA-event profile (separate, untimed pass)
+    eng.set_profiling(True)
+    device_step()
+    kt = eng.kernel_times()
+    eng.set_profiling(False)
+    gbytes, sbytes = round_bytes(stats, w["vd_bytes"], w["ed_bytes"], w["gather"])
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k)                      # L2 flush between timed steps
+            eng.restore_vertex_data()
+            ev[k][0].record(stream)
+            eng.set_active(lo, hi)
+            eng.run(w["max_iters"])
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = allreduce_max(world, float(sum(step_ms)))
+    all_edges = allreduce_sum(world, edges_per_run * args.steps)
+    value = all_edges / (total_ms / 1e3) / 1e9
+
+    # end to end through the C ABI with host buffers: initial vertex data
+    # H2D from pinned memory, run(), results D2H into the borrowed array
+    host_in = torch.from_numpy(init.view(np.uint8).copy()).pin_memory().numpy().view(init.dtype)
+    result = torch.empty(init.nbytes, dtype=torch.uint8).pin_memory().numpy().view(init.dtype)
+    e2e_eng = gas.GASEngine(w["program"], device=local, stream=stream.cuda_stream)
+    e2e_eng.set_graph(g.n_vertices, result, g.srcs, g.dsts, ed)
+    for _ in range(max(1, args.warmup)):
+        e2e_eng.set_vertex_data(host_in)
+        e2e_eng.set_active(lo, hi)
+        e2e_eng.run(w["max_iters"])
+        e2e_eng.get_results()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_eng.set_vertex_data(host_in)
+        e2e_eng.set_active(lo, hi)
+        e2e_eng.run(w["max_iters"])
+        e2e_eng.get_results()
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(world, time.perf_counter() - t0)
+    e2e_value = all_edges / e2e_s / 1e9
+    eng.get_results()  # device-resident run's result, into `init`
+    if not np.array_equal(init, result):
+        raise SystemExit("end-to-end result differs from the device-resident run")
+    nbytes = init.nbytes
+
+    peak, peak_kind = measured_peak()
+    gms, sms_ = kt["gather_ms"], kt["scatter_ms"]
+    dominant = "gather_apply" if gms >= sms_ else "scatter_activate"
+    dbytes = gbytes.sum() if dominant == "gather_apply" else sbytes.sum()
+    dms = gms if dominant == "gather_apply" else sms_
+    achieved = float(dbytes) / (dms / 1e3) / 1e9 if dms > 0 else 0.0
+    launches_per_step = 2 * rounds + (1 if w["gather"] else 0)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        port = oracle.port()
+        t0 = time.perf_counter()
+        st = cpu_run(port, w, args.workload)
+        cpu_s = time.perf_counter() - t0
+        cpu_edges = float(st["gathered"].sum() + st["scattered"].sum())
+        cpu = {"value": cpu_edges / (st["run_ns"] / 1e9) / 1e9, "unit": "GTEPS", "cores": 1,
+               "kind": "port",
+               "sample": f"one full run of the workload ({st['iterations']} rounds, "
+                         f"{cpu_s:.1f} s wall), run()+getResults() timed as bfs.cu:100-111"}
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    line = {
+        "metric": "GTEPS & %HBM roofline per algo", "value": value, "unit": "GTEPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32" if w["program"] != 4 else "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
+                   "n_vertices": g.n_vertices, "n_edges": g.n_edges, "seed": SEED,
+                   "rounds": rounds, "edges_traversed_per_run": edges_per_run,
+                   "l2": "flushed between timed steps (512 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": None,
+                     "kernel_ms_per_run": {"gather_apply": gms, "scatter_activate": sms_},
+                     "algorithmic_bytes_per_run": {"gather_apply": float(gbytes.sum()),
+                                                   "scatter_activate": float(sbytes.sum())}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "ms_per_step": 1e3 * e2e_s / args.steps},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sssp-grid1024")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

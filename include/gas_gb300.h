@@ -1,0 +1,185 @@
+/*
+ * gas_gb300.h -- C ABI of the GB300 Gather-Apply-Scatter engine.
+ *
+ * Two layers, both plain C (pointers, sizes, status codes; no C++ or torch
+ * types), exported from libgas_gb300.so:
+ *
+ *  1. The engine layer (gas_engine_*): one call per method of vertexAPI2's
+ *     GASEngineGPU (gpugas.h:74-773), for the built-in vertex programs
+ *     (BFS, SSSP, connected components, PageRank, personalised PageRank).
+ *     This is what an FFI binding (ctypes, cgo, JNI) of the reference path
+ *     would bind.
+ *
+ *  2. The core layer (gas_core_*, declared in gas_gb300_core.h): the
+ *     Program-independent half of the engine.  The C++ header
+ *     gas_gb300/gpugas.cuh drives it for user-written vertex programs,
+ *     whose gather/apply kernels are instantiated in the user's own
+ *     translation unit (Programs are compile-time types, as in gpugas.h).
+ *
+ * Every function returns a gas_status (0 = GAS_OK).  No function aborts the
+ * process; gas_last_error() gives a one-line description of the most recent
+ * failure on the calling thread.  An engine or state object is used by one
+ * host thread at a time.
+ */
+#ifndef GAS_GB300_H
+#define GAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GAS_API __attribute__((visibility("default")))
+#else
+#define GAS_API
+#endif
+
+typedef int32_t gas_status;
+enum {
+  GAS_OK = 0,
+  GAS_ERR_INVALID = 1,      /* bad argument (null pointer, id out of range, ...) */
+  GAS_ERR_OOM = 2,          /* device or host allocation failed                   */
+  GAS_ERR_CUDA = 3,         /* a CUDA runtime call failed                          */
+  GAS_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up                  */
+  GAS_ERR_STATE = 5,        /* call out of order (e.g. no graph set)               */
+  GAS_ERR_UNSUPPORTED = 6,  /* feature not available for this program / size       */
+  GAS_ERR_NO_DEVICE = 7     /* no CUDA device, or the device is not sm_103         */
+};
+
+/* Program ids of the built-in vertex programs (engine layer). */
+enum {
+  GAS_PROGRAM_BFS = 1,       /* bfs.cu:31-78                       VertexData int32 depth      */
+  GAS_PROGRAM_SSSP = 2,      /* sssp.cu:25-64                      VertexData int32, EdgeData int32 */
+  GAS_PROGRAM_CC = 3,        /* connected_component.cu:25-63       VertexData int32 label      */
+  GAS_PROGRAM_PAGERANK = 4,  /* pagerank.cu:27-73                  VertexData {float rank; int32 numOutEdges} */
+  GAS_PROGRAM_PPR = 5        /* personalised PageRank, alpha 0.15 (no reference counterpart)
+                                VertexData {float rank; int32 numOutEdges; float teleport} */
+};
+
+typedef struct gas_engine_s gas_engine;
+
+/* ---------------- engine layer (GASEngineGPU, gpugas.h) ------------------ */
+
+/* Replaces the GASEngineGPU constructor (gpugas.h:144-172), which bound the
+ * engine to device 0 and the default stream.  `stream` is a cudaStream_t
+ * (NULL = the legacy default stream). */
+GAS_API gas_status gas_engine_create(int32_t program, int32_t device, void *stream,
+                                     gas_engine **out);
+
+/* Replaces ~GASEngineGPU (gpugas.h:175-197). NULL is accepted. */
+GAS_API gas_status gas_engine_destroy(gas_engine *e);
+
+/* Replaces setGraph (gpugas.h:212-322): builds CSC (gather) and CSR
+ * (scatter) on the device from the edge list, sorts edge data into CSC order
+ * and copies vertex data to the device.  vertexData / edgeData are borrowed
+ * host arrays of the program's VertexData / EdgeData (either may be NULL,
+ * as in the reference); getResults writes back into them. */
+GAS_API gas_status gas_engine_set_graph(gas_engine *e, int32_t nVertices, void *vertexData,
+                                        int32_t nEdges, void *edgeData,
+                                        const int32_t *edgeListSrcs,
+                                        const int32_t *edgeListDsts);
+
+/* Replaces getResults (gpugas.h:329-338): copies vertex data (and edge
+ * data, in the caller's original edge order) back to the host arrays. */
+GAS_API gas_status gas_engine_get_results(gas_engine *e);
+
+/* Re-uploads vertex data from `host` (nVertices elements) without rebuilding
+ * the graph; the vertex-data half of setGraph (gpugas.h:221-226). */
+GAS_API gas_status gas_engine_set_vertex_data(gas_engine *e, const void *host);
+
+/* Replaces setActive (gpugas.h:342-349): active set = [start, end). */
+GAS_API gas_status gas_engine_set_active(gas_engine *e, int32_t vertexStart, int32_t vertexEnd);
+
+/* Replaces countActive (gpugas.h:353-356).  Waits for queued work. */
+GAS_API gas_status gas_engine_count_active(gas_engine *e, int32_t *nActive);
+
+/* Replaces gatherApply (gpugas.h:421-513).  Asynchronous. */
+GAS_API gas_status gas_engine_gather_apply(gas_engine *e, int32_t haveGather);
+
+/* Replaces scatterActivate (gpugas.h:669-751).  Asynchronous: the next
+ * active set is built on the device (no host round trip). */
+GAS_API gas_status gas_engine_scatter_activate(gas_engine *e, int32_t haveScatter);
+
+/* Replaces nextIter (gpugas.h:754-758).  nActive may be NULL (then the
+ * call does not wait); otherwise it waits and returns the new count. */
+GAS_API gas_status gas_engine_next_iter(gas_engine *e, int32_t *nActive);
+
+/* Replaces run (gpugas.h:764-772): iterate until no vertex is active, or
+ * for at most maxIters rounds when maxIters > 0.  iterations (may be NULL)
+ * receives the number of non-empty rounds executed. */
+GAS_API gas_status gas_engine_run(gas_engine *e, int32_t maxIters, int32_t *iterations);
+
+/* Replaces the BFS driver's setIterationCount<true> (bfs.cu:81-88,
+ * cudaMemcpyToSymbol of g_iterationCountGPU): the iteration number the
+ * built-in BFS program writes as depth on the next gatherApply. */
+GAS_API gas_status gas_engine_set_iteration(gas_engine *e, int32_t iteration);
+
+/* Per-round counts of the last run()/stepwise sequence since setActive:
+ * for round k, active[k] = |A_k|, gathered[k] = in-edges of A_k,
+ * ret[k] = vertices whose apply returned true, scattered[k] = their
+ * out-edges.  Arrays may be NULL; `capacity` bounds what is written.
+ * *rounds receives the number of rounds recorded. */
+GAS_API gas_status gas_engine_round_stats(gas_engine *e, int32_t capacity, int64_t *active,
+                                          int64_t *gathered, int64_t *ret,
+                                          int64_t *scattered, int32_t *rounds);
+
+/* Elapsed device time (ms, CUDA events on the engine's stream) of the most
+ * recent gas_engine_run call. */
+GAS_API gas_status gas_engine_last_run_ms(gas_engine *e, float *ms);
+
+/* Device-side copy of the current vertex data (saved once, restored any
+ * number of times, asynchronously on the engine's stream): repeated runs
+ * on a resident graph without a host round trip. */
+GAS_API gas_status gas_engine_save_vertex_data(gas_engine *e);
+GAS_API gas_status gas_engine_restore_vertex_data(gas_engine *e);
+
+/* Per-kernel timing of run(): when enabled, every gather/apply and
+ * scatter/activate launch of run() is bracketed by CUDA events on the
+ * engine's stream; gas_engine_kernel_times returns the summed device
+ * milliseconds and launch counts of the most recent run(). */
+GAS_API gas_status gas_engine_set_profiling(gas_engine *e, int32_t enabled);
+GAS_API gas_status gas_engine_kernel_times(gas_engine *e, float *gatherMs, float *scatterMs,
+                                           int32_t *gatherLaunches, int32_t *scatterLaunches);
+
+/* ---------------- status / diagnostics ---------------------------------- */
+GAS_API const char *gas_status_string(gas_status s);
+GAS_API const char *gas_last_error(void);
+/* 1 when a CUDA device with compute capability 10.3 is present. */
+GAS_API int32_t gas_device_supported(int32_t device);
+
+/* ---------------- synthetic graph generators (host) --------------------- */
+/* Edge lists are allocated by the library; release with gas_edge_list_free.
+ * weights is NULL unless requested. Output is sorted by (src, dst). */
+typedef struct {
+  int32_t nVertices;
+  int64_t nEdges;
+  int32_t *srcs;
+  int32_t *dsts;
+  int32_t *weights;
+} gas_edge_list;
+
+/* R-MAT (Chakrabarti et al. 2004): 2^scale vertices, edgeFactor*2^scale
+ * samples with quadrant probabilities a, b, c (d = 1-a-b-c), drawn from a
+ * counter-based SplitMix64 stream keyed by `seed`; no vertex permutation.
+ * Self-loops and duplicates are removed; symmetrize != 0 adds every
+ * reverse edge.  When wHi >= wLo >= 1, integer weights uniform in
+ * [wLo, wHi] are attached, equal in both directions of an edge. */
+GAS_API gas_status gas_gen_rmat(int32_t scale, int32_t edgeFactor, double a, double b, double c,
+                                uint64_t seed, int32_t symmetrize, int32_t wLo, int32_t wHi,
+                                gas_edge_list *out);
+
+/* rows x cols 4-neighbour lattice; each undirected edge deleted with
+ * probability pDelete; the largest connected component is kept and
+ * relabelled row-major to 0..V'-1; symmetric; weights as for R-MAT. */
+GAS_API gas_status gas_gen_grid(int32_t rows, int32_t cols, double pDelete, uint64_t seed,
+                                int32_t wLo, int32_t wHi, gas_edge_list *out);
+
+GAS_API void gas_edge_list_free(gas_edge_list *l);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

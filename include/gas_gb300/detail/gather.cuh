@@ -1,0 +1,372 @@
+// Program-templated gather+apply kernel of the GB300 GAS engine.
+//
+// Replaces the reference's gather pipeline -- edge-count scan, merge-path
+// partitions, kGatherMap writing one (key, value) pair per edge to global
+// memory, ReduceByKey and kApply (gpugas.h:421-513,
+// gpugas_kernels.cuh:53-151) -- by one kernel:
+//
+//   * tiles of GAS_GATHER_TILE merged items (active vertices + their
+//     in-edges) whose merge-path splits were written by whoever built the
+//     frontier (block_append) -- no partition pass;
+//   * per thread GAS_GATHER_ITEMS consecutive items: all in-edge source
+//     loads, then all gatherMap loads, issued before any reduction (ILP);
+//   * thread-sequential fold + block-wide segmented scan for vertices that
+//     straddle threads, and a decoupled look-back over published tile
+//     aggregates for vertices that straddle tiles;
+//   * apply() on a register copy of the vertex, written to vertexNew[i]
+//     (committed by the scatter kernel, so every gather of this round reads
+//     the previous round's values: the bulk-synchronous semantics of
+//     refgas.h:143-167);
+//   * vertices whose apply returned true are appended to the scatter list
+//     with their out-degree prefix and the scatter kernel's tile splits.
+#pragma once
+
+#include <type_traits>
+
+#include "primitives.cuh"
+
+namespace gas {
+namespace detail {
+
+constexpr int kGNT = GAS_GATHER_THREADS;
+constexpr int kGVT = GAS_GATHER_ITEMS;
+constexpr int kGTILE = GAS_GATHER_TILE;
+constexpr int kSTILE = GAS_SCATTER_TILE;
+
+// apply() with or without the iteration number.  The reference BFS reads
+// the iteration from a __constant__ set by the driver (bfs.cu:28,63,85);
+// programs may instead take it as a third argument.
+template <class P>
+struct ApplyTakesIteration {
+  template <class Q>
+  static auto test(int) -> decltype(Q::apply((typename Q::VertexData *)0,
+                                             typename Q::GatherResult(), 0),
+                                    std::true_type());
+  template <class Q>
+  static std::false_type test(...);
+  static constexpr bool value = decltype(test<P>(0))::value;
+};
+
+template <class P>
+__device__ __forceinline__ bool call_apply(typename P::VertexData *v,
+                                           const typename P::GatherResult &g, int iteration,
+                                           std::true_type) {
+  return P::apply(v, g, iteration);
+}
+template <class P>
+__device__ __forceinline__ bool call_apply(typename P::VertexData *v,
+                                           const typename P::GatherResult &g, int,
+                                           std::false_type) {
+  return P::apply(v, g);
+}
+template <class P>
+__device__ __forceinline__ bool do_apply(typename P::VertexData *v,
+                                         const typename P::GatherResult &g, int iteration) {
+  return call_apply<P>(v, g, iteration,
+                       std::integral_constant<bool, ApplyTakesIteration<P>::value>());
+}
+
+template <class P>
+__device__ __forceinline__ const typename P::EdgeData *edge_ptr(const void *ed, int32_t e) {
+  if (std::is_empty<typename P::EdgeData>::value) return nullptr;
+  return reinterpret_cast<const typename P::EdgeData *>(ed) + e;
+}
+
+template <class P>
+struct GatherSmem {
+  int32_t end[kGTILE];       // tile-local edge index at which vertex i0+m ends
+  int32_t vid[kGTILE + 1];   // vertex id of frontier entry i0+m
+  int32_t base[kGTILE + 1];  // CSC position = frontier edge index + base
+  SegScanSmem<typename P::GatherResult, kGNT> seg;
+  AppendSmem<kGNT, kGVT> app;
+  int32_t headPre;
+  unsigned lookHas;
+  typename P::GatherResult lookVal;
+  int32_t tile;
+};
+
+// Current frontier size: (n, total in-edges).
+__device__ __forceinline__ void frontier_size(const gas_gather_args &a, int &n, int &T) {
+  if (a.rangeMode) {
+    n = a.rangeCount;
+    T = a.inOffsets[a.rangeStart + a.rangeCount] - a.rangeBase;
+  } else {
+    unsigned long long c = *a.frontCount;
+    n = (int)(c >> 32);
+    T = (int)(c & 0xffffffffull);
+    if (n > a.capacity) n = a.capacity;  // only after a reported overflow
+  }
+}
+
+template <class P>
+__device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, GatherSmem<P> &sm) {
+  typedef typename P::VertexData VD;
+  typedef typename P::GatherResult GR;
+  const int tid = threadIdx.x;
+  const long long total = (long long)n + T;
+  const int d0 = t * kGTILE;
+  const int d1 = (int)min((long long)d0 + kGTILE, total);
+  const int i0 = a.frontSplit[t];
+  const int i1 = (d1 == total) ? n : a.frontSplit[t + 1];
+  const int j0 = d0 - i0, j1 = d1 - i1;
+  const int nb = i1 - i0;  // vertices ending in this tile
+  const int na = j1 - j0;  // edges in this tile
+  const int nload = nb + (i1 < n ? 1 : 0);
+  const VD *vd = reinterpret_cast<const VD *>(a.vertexData);
+
+  for (int m = tid; m < nload; m += kGNT) {
+    const int i = i0 + m;
+    int v, pre, end;
+    if (a.rangeMode) {
+      v = a.rangeStart + i;
+      pre = a.inOffsets[v] - a.rangeBase;
+      end = a.inOffsets[v + 1] - a.rangeBase;
+    } else {
+      v = a.frontVid[i];
+      pre = a.frontPre[i];
+      end = (i + 1 < n) ? a.frontPre[i + 1] : T;
+    }
+    sm.vid[m] = v;
+    sm.base[m] = a.inOffsets[v] - pre;
+    if (m < nb) sm.end[m] = end - j0;
+    if (m == 0) sm.headPre = pre;
+  }
+  __syncthreads();
+
+  // ---- merge-path walk of this thread's items
+  const int tileItems = d1 - d0;
+  const int dl = tid * kGVT;
+  int bi = 0;
+  if (dl < tileItems) {
+    int lo = max(0, dl - na), hi = min(dl, nb);
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (sm.end[mid - 1] <= dl - mid)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    bi = lo;
+  }
+  int aj = dl - bi;
+  int kind[kGVT], vloc[kGVT], phys[kGVT];
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v) {
+    kind[v] = 0;
+    vloc[v] = 0;
+    phys[v] = 0;
+    if (dl + v < tileItems) {
+      if (bi < nb && (aj >= na || sm.end[bi] <= aj)) {
+        kind[v] = 2;
+        vloc[v] = bi;
+        ++bi;
+      } else {
+        kind[v] = 1;
+        vloc[v] = bi;
+        phys[v] = j0 + aj + sm.base[bi];
+        ++aj;
+      }
+    }
+  }
+
+  // ---- loads first (independent), then gatherMap values
+  int src[kGVT];
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v) src[v] = (kind[v] == 1) ? __ldg(a.inSources + phys[v]) : 0;
+  GR val[kGVT];
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v)
+    if (kind[v] == 1)
+      val[v] = P::gatherMap(vd + sm.vid[vloc[v]], vd + src[v], edge_ptr<P>(a.edgeData, phys[v]));
+
+  // ---- thread-sequential fold; seg_*[v] holds the segment ending at item v
+  unsigned has = 0u;
+  GR acc;
+  bool segHas[kGVT];
+  GR segVal[kGVT];
+  unsigned anyEnd = 0u;
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v) {
+    segHas[v] = false;
+    if (kind[v] == 1) {
+      acc = has ? P::gatherReduce(acc, val[v]) : val[v];
+      has = 1u;
+    } else if (kind[v] == 2) {
+      segHas[v] = has != 0u;
+      segVal[v] = acc;
+      has = 0u;
+      anyEnd = 1u;
+    }
+  }
+  SegVal<GR> mine;
+  mine.end = anyEnd;
+  mine.has = has;
+  mine.val = acc;
+  SegVal<GR> excl, tot;
+  block_seg_scan<P, GR, kGNT>(mine, excl, tot, sm.seg);
+
+  // ---- publish this tile's tail aggregate for the tiles after it
+  if (tid == kGNT - 1 && tot.has) {
+    reinterpret_cast<GR *>(a.carryVal)[t] = tot.val;
+    __threadfence();
+    st_release(a.carryFlag + t, a.epoch);
+  }
+  // ---- look-back for a first vertex that started in an earlier tile
+  const bool headSplit = nb > 0 && sm.headPre < j0;
+  if (tid < 32) {
+    if (headSplit) {
+      const int ts = (int)(((long long)sm.headPre + i0) / kGTILE);
+      unsigned lh = 0u;
+      GR lv;
+      for (int c0 = ts; c0 < t; c0 += 32) {
+        const int ti = c0 + tid;
+        const int cnt = min(32, t - c0);
+        unsigned h = 0u;
+        GR x;
+        if (ti < t) {
+          if (wait_flag(a.carryFlag + ti, a.epoch, a.errWord)) {
+            x = load_cg(reinterpret_cast<const GR *>(a.carryVal) + ti);
+            h = 1u;
+          }
+        }
+        // ordered tree reduction over lanes 0..cnt-1
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          unsigned oh = __shfl_down_sync(kFullMask, h, d);
+          GR ox = shfl_down_any(x, d);
+          if ((tid & (2 * d - 1)) == 0 && tid + d < cnt) {
+            if (oh) {
+              x = h ? P::gatherReduce(x, ox) : ox;
+              h = 1u;
+            }
+          }
+        }
+        if (tid == 0 && h) {
+          lv = lh ? P::gatherReduce(lv, x) : x;
+          lh = 1u;
+        }
+      }
+      if (tid == 0) {
+        sm.lookHas = lh;
+        if (lh) sm.lookVal = lv;
+      }
+    } else if (tid == 0) {
+      sm.lookHas = 0u;
+    }
+  }
+  __syncthreads();
+
+  // ---- prefix for this thread's first vertex end
+  unsigned preHas = 0u;
+  GR preVal;
+  if (!excl.end && headSplit && sm.lookHas) {
+    preVal = sm.lookVal;
+    preHas = 1u;
+  }
+  if (excl.has) {
+    preVal = preHas ? P::gatherReduce(preVal, excl.val) : excl.val;
+    preHas = 1u;
+  }
+  bool firstDone = false;
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v) {
+    if (kind[v] == 2 && !firstDone) {
+      firstDone = true;
+      if (preHas) {
+        segVal[v] = segHas[v] ? P::gatherReduce(preVal, segVal[v]) : preVal;
+        segHas[v] = true;
+      }
+    }
+  }
+
+  // ---- apply and collect vertices that activate their out-neighbours
+  const GR gz = P::gatherZero;
+  bool ok[kGVT];
+  int32_t ovid[kGVT], odeg[kGVT];
+  VD *vnew = reinterpret_cast<VD *>(a.vertexNew);
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v) {
+    ok[v] = false;
+    ovid[v] = 0;
+    odeg[v] = 0;
+    if (kind[v] == 2) {
+      const int m = vloc[v];
+      const int32_t vx = sm.vid[m];
+      GR g = gz;
+      if (segHas[v]) g = P::gatherReduce(gz, segVal[v]);
+      VD tmp = vd[vx];
+      const bool r = do_apply<P>(&tmp, g, a.iteration);
+      vnew[i0 + m] = tmp;
+      if (r) {
+        ok[v] = true;
+        ovid[v] = vx;
+        odeg[v] = a.outOffsets[vx + 1] - a.outOffsets[vx];
+      }
+    }
+  }
+  block_append<kGNT, kGVT, kSTILE>(ok, ovid, odeg, a.scatVid, a.scatPre, a.scatSplit,
+                                   a.maxScatTiles, a.scatCount, a.capacity, a.errWord, sm.app);
+}
+
+// apply only (gatherApply(false), gpugas.h:503-512): one thread per active
+// vertex, vertex data updated in place.
+template <class P>
+__device__ void apply_tile(const gas_gather_args &a, int t, int n, GatherSmem<P> &sm) {
+  typedef typename P::VertexData VD;
+  typedef typename P::GatherResult GR;
+  VD *vd = reinterpret_cast<VD *>(a.vertexData);
+  const GR gz = P::gatherZero;
+  bool ok[kGVT];
+  int32_t ovid[kGVT], odeg[kGVT];
+#pragma unroll
+  for (int v = 0; v < kGVT; ++v) {
+    ok[v] = false;
+    ovid[v] = 0;
+    odeg[v] = 0;
+    const int i = t * kGTILE + v * kGNT + threadIdx.x;
+    if (i < n) {
+      const int32_t vx = a.rangeMode ? a.rangeStart + i : a.frontVid[i];
+      VD tmp = vd[vx];
+      const bool r = do_apply<P>(&tmp, gz, a.iteration);
+      vd[vx] = tmp;
+      if (r) {
+        ok[v] = true;
+        ovid[v] = vx;
+        odeg[v] = a.outOffsets[vx + 1] - a.outOffsets[vx];
+      }
+    }
+  }
+  block_append<kGNT, kGVT, kSTILE>(ok, ovid, odeg, a.scatVid, a.scatPre, a.scatSplit,
+                                   a.maxScatTiles, a.scatCount, a.capacity, a.errWord, sm.app);
+}
+
+// Persistent-style grid: blocks take tiles in order from a counter, so a
+// tile whose look-back waits on earlier tiles only waits on running CTAs.
+template <class P>
+__global__ void __launch_bounds__(kGNT) gather_apply_kernel(const gas_gather_args a) {
+  __shared__ GatherSmem<P> sm;
+  int n, T;
+  frontier_size(a, n, T);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *a.resetCount = 0ull;
+    *a.resetTile = 0u;
+    if (a.statSlot) a.statSlot[0] = ((unsigned long long)n << 32) | (unsigned)T;
+  }
+  const long long items = a.haveGather ? (long long)n + T : (long long)n;
+  const int ntiles = (int)((items + kGTILE - 1) / kGTILE);
+  for (;;) {
+    if (threadIdx.x == 0) sm.tile = (int)atomicAdd(a.tileCounter, 1u);
+    __syncthreads();
+    const int t = sm.tile;
+    __syncthreads();
+    if (t >= ntiles) break;
+    if (a.haveGather)
+      gather_tile<P>(a, t, n, T, sm);
+    else
+      apply_tile<P>(a, t, n, sm);
+    __syncthreads();
+  }
+}
+
+}  // namespace detail
+}  // namespace gas

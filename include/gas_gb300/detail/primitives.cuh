@@ -1,0 +1,312 @@
+// Device primitives shared by the gather, apply and scatter kernels.
+//
+// - word-wise warp shuffles for any trivially copyable type;
+// - block-wide scans (u64 sums; segmented pairs for partial reductions);
+// - bounded acquire/release flag helpers for cross-tile look-back;
+// - block_append: reserves space in a frontier list with one packed 64-bit
+//   atomic per tile and writes merge-path split hints for the consumer's
+//   tiles, so the next kernel needs no partition search.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../gas_gb300_core.h"
+
+namespace gas {
+namespace detail {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+// ~0.5 s of polling before a look-back wait reports GAS_DEVERR_TIMEOUT
+constexpr unsigned kSpinLimit = 1u << 22;
+
+template <typename T>
+__device__ __forceinline__ T shfl_up_any(const T &v, int delta) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k) w[k] = __shfl_up_sync(kFullMask, w[k], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_down_any(const T &v, int delta) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k) w[k] = __shfl_down_sync(kFullMask, w[k], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_any(const T &v, int lane) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k) w[k] = __shfl_sync(kFullMask, w[k], lane);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+// L1-bypassing load of any type (values published by other CTAs).
+template <typename T>
+__device__ __forceinline__ T load_cg(const T *p) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  uint32_t w[W];
+  if (sizeof(T) % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < W; ++k) w[k] = __ldcg(reinterpret_cast<const unsigned *>(p) + k);
+  } else {
+    memcpy(w, (const void *)p, sizeof(T));
+  }
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits (bounded) until *flag == want.  Returns false and sets
+// GAS_DEVERR_TIMEOUT in *err when the limit is reached.
+__device__ __forceinline__ bool wait_flag(const unsigned *flag, unsigned want, unsigned *err) {
+  unsigned spins = 0;
+  while (ld_acquire(flag) != want) {
+    if (++spins > kSpinLimit) {
+      atomicOr(err, GAS_DEVERR_TIMEOUT);
+      return false;
+    }
+    __nanosleep(64);
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive scan of unsigned 64-bit sums.
+template <int NT>
+struct ScanU64Smem {
+  unsigned long long warp[NT / 32];
+  unsigned long long total;
+};
+
+template <int NT>
+__device__ __forceinline__ void block_exclusive_scan_u64(unsigned long long x,
+                                                         unsigned long long &excl,
+                                                         unsigned long long &total,
+                                                         ScanU64Smem<NT> &sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    unsigned long long o = __shfl_up_sync(kFullMask, incl, d);
+    if (lane >= d) incl += o;
+  }
+  if (lane == 31) sm.warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < NT / 32 ? sm.warp[lane] : 0ull;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      unsigned long long o = __shfl_up_sync(kFullMask, w, d);
+      if (lane >= d) w += o;
+    }
+    if (lane < NT / 32) sm.warp[lane] = w;
+    if (lane == NT / 32 - 1) sm.total = w;
+  }
+  __syncthreads();
+  unsigned long long wpre = warp > 0 ? sm.warp[warp - 1] : 0ull;
+  excl = wpre + incl - x;
+  total = sm.total;
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Segmented partial reductions.  A SegVal is the state flowing between
+// consecutive items: `end` = a vertex boundary occurred inside, `has` = val
+// holds a reduction of at least one gathered edge value.
+template <typename T>
+struct SegVal {
+  unsigned end;
+  unsigned has;
+  T val;
+};
+
+template <class P, typename T>
+__device__ __forceinline__ SegVal<T> seg_combine(const SegVal<T> &a, const SegVal<T> &b) {
+  if (b.end) return b;
+  SegVal<T> r;
+  r.end = a.end;
+  if (!a.has) {
+    r.has = b.has;
+    r.val = b.val;
+  } else if (!b.has) {
+    r.has = 1u;
+    r.val = a.val;
+  } else {
+    r.has = 1u;
+    r.val = P::gatherReduce(a.val, b.val);
+  }
+  return r;
+}
+
+template <typename T, int NT>
+struct SegScanSmem {
+  SegVal<T> warp[NT / 32];
+};
+
+// Inclusive block scan with seg_combine; returns the exclusive prefix of
+// this thread in `excl` and the block aggregate in `total`.
+template <class P, typename T, int NT>
+__device__ __forceinline__ void block_seg_scan(const SegVal<T> &x, SegVal<T> &excl,
+                                               SegVal<T> &total, SegScanSmem<T, NT> &sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  SegVal<T> incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    SegVal<T> o;
+    o.end = __shfl_up_sync(kFullMask, incl.end, d);
+    o.has = __shfl_up_sync(kFullMask, incl.has, d);
+    o.val = shfl_up_any(incl.val, d);
+    if (lane >= d) incl = seg_combine<P>(o, incl);
+  }
+  if (lane == 31) sm.warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    SegVal<T> w;
+    if (lane < NT / 32) {
+      w = sm.warp[lane];
+    } else {
+      w.end = 0u;
+      w.has = 0u;
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      SegVal<T> o;
+      o.end = __shfl_up_sync(kFullMask, w.end, d);
+      o.has = __shfl_up_sync(kFullMask, w.has, d);
+      o.val = shfl_up_any(w.val, d);
+      if (lane >= d) w = seg_combine<P>(o, w);
+    }
+    if (lane < NT / 32) sm.warp[lane] = w;
+  }
+  __syncthreads();
+  SegVal<T> wpre;
+  if (warp > 0) {
+    wpre = sm.warp[warp - 1];
+  } else {
+    wpre.end = 0u;
+    wpre.has = 0u;
+  }
+  SegVal<T> prev;
+  prev.end = __shfl_up_sync(kFullMask, incl.end, 1);
+  prev.has = __shfl_up_sync(kFullMask, incl.has, 1);
+  prev.val = shfl_up_any(incl.val, 1);
+  if (lane == 0) {
+    excl = wpre;
+  } else {
+    excl = (warp > 0) ? seg_combine<P>(wpre, prev) : prev;
+  }
+  total = sm.warp[NT / 32 - 1];
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// block_append: every thread offers up to K (vertex, degree) entries in
+// static slots ok[k]/vid[k]/deg[k].  The block reserves (count, degree sum)
+// with one atomicAdd on the packed counter (count << 32 | degree sum), so
+// positions and exclusive degree prefixes of all batches agree.  It then
+// writes, for every consumer tile boundary b = t*TILE falling inside this
+// batch's merged (entries + degrees) range, the number of entries whose
+// end precedes b -- the merge-path split of tile t.
+template <int NT, int K>
+struct AppendSmem {
+  int32_t vid[NT * K + 1];
+  int32_t pre[NT * K + 1];
+  ScanU64Smem<NT> scan;
+  unsigned long long base;
+};
+
+template <int NT, int K, int TILE>
+__device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t (&vid)[K],
+                                             const int32_t (&deg)[K], int32_t *outVid,
+                                             int32_t *outPre, int32_t *outSplit,
+                                             int32_t maxSplit,
+                                             unsigned long long *outCount, int32_t capacity,
+                                             unsigned *errWord, AppendSmem<NT, K> &sm) {
+  unsigned cnt = 0, esum = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (ok[k]) {
+      ++cnt;
+      esum += (unsigned)deg[k];
+    }
+  unsigned long long mine = ((unsigned long long)cnt << 32) | esum;
+  unsigned long long excl, total;
+  block_exclusive_scan_u64<NT>(mine, excl, total, sm.scan);
+  if (total == 0ull) return;  // block-uniform
+  if (threadIdx.x == 0) sm.base = atomicAdd(outCount, total);
+  int off = (int)(excl >> 32);
+  int eoff = (int)(excl & 0xffffffffull);
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (ok[k]) {
+      sm.vid[off] = vid[k];
+      sm.pre[off] = eoff;
+      ++off;
+      eoff += deg[k];
+    }
+  const int R = (int)(total >> 32);
+  const int Esum = (int)(total & 0xffffffffull);
+  if (threadIdx.x == 0) sm.pre[R] = Esum;
+  __syncthreads();
+  const unsigned long long base = sm.base;
+  const long long qpos = (long long)(base >> 32);
+  const long long epos = (long long)(base & 0xffffffffull);
+  if (qpos + R > capacity) {
+    if (threadIdx.x == 0) atomicOr(errWord, GAS_DEVERR_CAPACITY);
+    __syncthreads();
+    return;
+  }
+  for (int m = threadIdx.x; m < R; m += NT) {
+    outVid[qpos + m] = sm.vid[m];
+    outPre[qpos + m] = (int32_t)(epos + sm.pre[m]);
+  }
+  // split hints for boundaries b in [D, D + R + Esum)
+  const long long D = qpos + epos;
+  const long long Dend = D + R + Esum;
+  const long long tFirst = (D + TILE - 1) / TILE;
+  const long long tLast = (Dend - 1) / TILE;
+  for (long long tb = tFirst + threadIdx.x; tb <= tLast; tb += NT) {
+    const long long b = tb * TILE - D;  // local diagonal of the boundary
+    // count entries m whose end (local diagonal pre[m+1] + m) is < b
+    int lo = 0, hi = R;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if ((long long)sm.pre[mid + 1] + mid < b)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (tb < maxSplit) outSplit[tb] = (int32_t)(qpos + lo);
+  }
+  __syncthreads();
+}
+
+}  // namespace detail
+}  // namespace gas

@@ -1,0 +1,173 @@
+// gpugas.cuh -- drop-in replacement for vertexAPI2's gpugas.h on GB300.
+//
+// A user vertex Program (VertexData / EdgeData / GatherResult, gatherZero,
+// gatherMap, gatherReduce, apply, scatter) runs unchanged on
+//
+//     GASEngineGPU<Program, Int = int32_t, sortEdgesForGather = true>
+//
+// with the reference's methods (gpugas.h:212-772): setGraph, getResults,
+// setActive, countActive, gatherApply, scatterActivate, nextIter, run.
+// Include this header from a .cu file compiled for sm_103a and link
+// libgas_gb300.so.  The Program's gather+apply kernel is instantiated here,
+// in the caller's translation unit; graph build, frontier and scatter live
+// in the library behind the C ABI of gas_gb300_core.h.
+//
+// Differences from the reference, all additive:
+//   * the constructor takes a device and stream (the reference hard-codes
+//     device 0 and the default stream, gpugas.h:171);
+//   * errors are not fatal: every method records a status, read with
+//     lastStatus() / lastError();
+//   * runFor(maxIters) bounds run(); apply() may take the round number as a
+//     third argument; a Program may declare `static constexpr bool
+//     haveGather = false` to make run() skip the gather (as bfs.cu does by
+//     calling gatherApply(false));
+//   * getResults() returns edge data in the caller's original order (the
+//     reference copies CSC-sorted data back, gpugas.h:333-336).
+// gatherZero must be usable in device code (constexpr or an integral
+// static const).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "../gas_gb300_core.h"
+#include "detail/gather.cuh"
+
+namespace gas {
+
+template <class P>
+struct ProgramHaveGather {
+  template <class Q>
+  static constexpr bool get(decltype(Q::haveGather) *) {
+    return Q::haveGather;
+  }
+  template <class Q>
+  static constexpr bool get(...) {
+    return true;
+  }
+  static constexpr bool value = get<P>(nullptr);
+};
+
+template <typename Program, typename Int = int32_t, bool sortEdgesForGather = true>
+class EngineGPU {
+  static_assert(std::is_same<Int, int32_t>::value, "vertex and edge ids are int32");
+
+ public:
+  typedef typename Program::VertexData VertexData;
+  typedef typename Program::EdgeData EdgeData;
+  typedef typename Program::GatherResult GatherResult;
+
+  explicit EngineGPU(int device = 0, cudaStream_t stream = 0) {
+    status_ = gas_core_create(device, (void *)stream, &core_);
+  }
+  ~EngineGPU() { gas_core_destroy(core_); }
+  EngineGPU(const EngineGPU &) = delete;
+  EngineGPU &operator=(const EngineGPU &) = delete;
+
+  // gpugas.h:212-322
+  void setGraph(Int nVertices, VertexData *vertexData, Int nEdges, EdgeData *edgeData,
+                const Int *edgeListSrcs, const Int *edgeListDsts) {
+    vdHost_ = vertexData;
+    edHost_ = edgeData;
+    const int32_t eb = kEdgeBytes;
+    if (!note(gas_core_set_graph(core_, nVertices, nEdges, edgeListSrcs, edgeListDsts,
+                                 eb ? (const void *)edgeData : nullptr, eb,
+                                 (int32_t)sizeof(VertexData), (int32_t)sizeof(GatherResult))))
+      return;
+    if (vertexData) note(gas_core_upload_vertex_data(core_, vertexData));
+  }
+
+  // gpugas.h:329-338
+  void getResults() {
+    if (vdHost_ && !note(gas_core_download_vertex_data(core_, vdHost_))) return;
+    if (edHost_ && kEdgeBytes) note(gas_core_download_edge_data(core_, edHost_));
+  }
+
+  // gpugas.h:342-349
+  void setActive(Int vertexStart, Int vertexEnd) {
+    note(gas_core_set_active(core_, vertexStart, vertexEnd));
+  }
+
+  // gpugas.h:353-356
+  Int countActive() {
+    int32_t n = 0;
+    if (!note(gas_core_count_active(core_, &n))) return 0;
+    return n;
+  }
+
+  // gpugas.h:421-513
+  void gatherApply(bool haveGather = true) {
+    note(gas_core_gather_apply(core_, haveGather ? 1 : 0, &launch, this));
+  }
+
+  // gpugas.h:669-751.  Program::scatter is not called, as in the
+  // reference's GPU engine (gpugas.h:666-668).
+  void scatterActivate(bool haveScatter = true) {
+    (void)haveScatter;
+    note(gas_core_scatter_activate(core_));
+  }
+
+  // gpugas.h:754-758
+  Int nextIter() {
+    if (!note(gas_core_next_iter(core_))) return 0;
+    return countActive();
+  }
+
+  // gpugas.h:764-772
+  void run() { runFor(0); }
+
+  // run() bounded to maxIters rounds (0 = until no vertex is active);
+  // returns the number of rounds executed.
+  int32_t runFor(int32_t maxIters) {
+    int32_t it = 0;
+    note(gas_core_run(core_, maxIters, ProgramHaveGather<Program>::value ? 1 : 0, &launch, this,
+                      &it));
+    return it;
+  }
+
+  // Round number handed to apply(v, g, round) by the stepwise API.
+  void setIteration(int32_t it) { note(gas_core_set_iteration(core_, it)); }
+
+  gas_status lastStatus() const { return status_; }
+  const char *lastError() const { return gas_last_error(); }
+  gas_core *core() { return core_; }
+
+ private:
+  static constexpr int32_t kEdgeBytes =
+      std::is_empty<EdgeData>::value ? 0 : (int32_t)sizeof(EdgeData);
+
+  bool note(gas_status s) {
+    status_ = s;
+    return s == GAS_OK;
+  }
+
+  static gas_status launch(void *user, const gas_gather_args *a, void *stream) {
+    EngineGPU *self = static_cast<EngineGPU *>(user);
+    if (self->grid_ == 0) {
+      int dev = 0, sms = 0, per = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per, detail::gather_apply_kernel<Program>, detail::kGNT, 0);
+      self->grid_ = (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
+    }
+    detail::gather_apply_kernel<Program>
+        <<<self->grid_, detail::kGNT, 0, (cudaStream_t)stream>>>(*a);
+    return cudaGetLastError() == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
+  }
+
+  gas_core *core_ = nullptr;
+  gas_status status_ = GAS_OK;
+  VertexData *vdHost_ = nullptr;
+  EdgeData *edHost_ = nullptr;
+  int grid_ = 0;
+};
+
+}  // namespace gas
+
+#ifndef GAS_GB300_NO_GLOBAL_NAME
+// Same name and template parameters as gpugas.h:74-77.
+template <typename Program, typename Int = int32_t, bool sortEdgesForGather = true>
+using GASEngineGPU = gas::EngineGPU<Program, Int, sortEdgesForGather>;
+#endif

@@ -1,0 +1,143 @@
+/*
+ * gas_gb300_core.h -- core layer of the GB300 GAS engine's C ABI.
+ *
+ * The Program-independent half of the engine (the parts of gpugas.h that do
+ * not call user code): device CSC/CSR construction (setGraph,
+ * gpugas.h:212-322), the active frontier (setActive / countActive,
+ * gpugas.h:342-356), scatter-activate and frontier rebuild
+ * (gpugas.h:669-751) and the iteration loop (gpugas.h:754-772).
+ *
+ * The Program-dependent gather+apply kernel is compiled in the caller's
+ * translation unit (gas_gb300/gpugas.cuh) and launched through the
+ * callback given to gas_core_gather_apply / gas_core_run; its arguments are
+ * the plain struct gas_gather_args below.
+ */
+#ifndef GAS_GB300_CORE_H
+#define GAS_GB300_CORE_H
+
+#include "gas_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Tile geometry shared by the core and header-instantiated kernels:
+ * a gather tile covers GAS_GATHER_TILE merged items (active vertices plus
+ * their in-edges), a scatter tile GAS_SCATTER_TILE items. */
+#define GAS_GATHER_THREADS 256
+#define GAS_GATHER_ITEMS 8
+#define GAS_GATHER_TILE (GAS_GATHER_THREADS * GAS_GATHER_ITEMS)
+#define GAS_SCATTER_THREADS 256
+#define GAS_SCATTER_ITEMS 8
+#define GAS_SCATTER_TILE (GAS_SCATTER_THREADS * GAS_SCATTER_ITEMS)
+
+/* Device error bits (gas_gather_args.errWord). */
+#define GAS_DEVERR_TIMEOUT 1u    /* bounded look-back wait gave up */
+#define GAS_DEVERR_CAPACITY 2u   /* a queue would have overflowed  */
+
+/* Arguments of one gather+apply launch (device pointers). */
+typedef struct {
+  /* graph: CSC for gather, CSR offsets for out-degrees */
+  int32_t nVertices;
+  int32_t nEdges;
+  const int32_t *inOffsets;   /* [nVertices+1] */
+  const int32_t *inSources;   /* [nEdges]      */
+  const int32_t *outOffsets;  /* [nVertices+1] */
+  const void *edgeData;       /* CSC order, NULL when EdgeData is empty */
+  /* vertex data: gather reads vertexData; apply writes vertexNew[i] for
+   * frontier position i (committed by scatter), or vertexData in place
+   * when haveGather == 0 */
+  void *vertexData;
+  void *vertexNew;
+  /* current frontier: range [rangeStart, rangeStart+n) or a list */
+  int32_t rangeMode;
+  int32_t rangeStart;
+  int32_t rangeCount;
+  int32_t rangeBase;          /* inOffsets[rangeStart] */
+  const int32_t *frontVid;    /* list mode: vertex ids                    */
+  const int32_t *frontPre;    /* list mode: exclusive prefix of in-degree */
+  const unsigned long long *frontCount; /* list mode: (n << 32) | total in-edges */
+  const int32_t *frontSplit;  /* gather-tile merge-path splits            */
+  /* scatter list appended by this launch */
+  int32_t *scatVid;
+  int32_t *scatPre;
+  int32_t *scatSplit;
+  unsigned long long *scatCount;
+  int32_t capacity;           /* capacity of scatVid / frontVid lists     */
+  int32_t maxScatTiles;
+  /* counters this launch resets for the following scatter */
+  unsigned long long *resetCount;
+  unsigned int *resetTile;
+  /* dynamic tile counter of this launch */
+  unsigned int *tileCounter;
+  /* cross-tile partial reductions (look-back) */
+  void *carryVal;
+  unsigned int *carryFlag;
+  unsigned int epoch;
+  /* misc */
+  unsigned int *errWord;
+  unsigned long long *statSlot; /* round statistics slot (may be NULL) */
+  int32_t iteration;
+  int32_t haveGather;
+} gas_gather_args;
+
+typedef struct gas_core_s gas_core;
+
+/* Launches the caller's gather+apply kernel for `args` on `stream`. */
+typedef gas_status (*gas_gather_launch_fn)(void *user, const gas_gather_args *args,
+                                           void *stream);
+
+GAS_API gas_status gas_core_create(int32_t device, void *stream, gas_core **out);
+GAS_API gas_status gas_core_destroy(gas_core *c);
+GAS_API gas_status gas_core_stream(gas_core *c, void **stream);
+
+/* setGraph: builds CSC+CSR on the device, sorts edge data (edgeBytes per
+ * edge, may be 0) into CSC order and allocates per-vertex state for the
+ * given VertexData / GatherResult sizes. */
+GAS_API gas_status gas_core_set_graph(gas_core *c, int32_t nVertices, int32_t nEdges,
+                                      const int32_t *srcs, const int32_t *dsts,
+                                      const void *edgeData, int32_t edgeBytes,
+                                      int32_t vertexBytes, int32_t gatherBytes);
+
+GAS_API gas_status gas_core_upload_vertex_data(gas_core *c, const void *host);
+GAS_API gas_status gas_core_download_vertex_data(gas_core *c, void *host);
+/* Edge data in the caller's original edge-list order. */
+GAS_API gas_status gas_core_download_edge_data(gas_core *c, void *host);
+/* Device pointer of the vertex data array. */
+GAS_API gas_status gas_core_vertex_data(gas_core *c, void **dev);
+
+GAS_API gas_status gas_core_set_active(gas_core *c, int32_t start, int32_t end);
+GAS_API gas_status gas_core_count_active(gas_core *c, int32_t *n);
+GAS_API gas_status gas_core_set_iteration(gas_core *c, int32_t iteration);
+
+/* One gatherApply: fills gas_gather_args and calls `launch`. */
+GAS_API gas_status gas_core_gather_apply(gas_core *c, int32_t haveGather,
+                                         gas_gather_launch_fn launch, void *user);
+/* One scatterActivate (commits apply's vertex data, expands out-edges of
+ * vertices whose apply returned true, builds the next frontier). */
+GAS_API gas_status gas_core_scatter_activate(gas_core *c);
+GAS_API gas_status gas_core_next_iter(gas_core *c);
+
+/* run(): rounds of gatherApply/scatterActivate/nextIter until no vertex is
+ * active (or maxIters rounds when maxIters > 0), without a host round trip
+ * per round. */
+GAS_API gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
+                                gas_gather_launch_fn launch, void *user,
+                                int32_t *iterations);
+
+GAS_API gas_status gas_core_round_stats(gas_core *c, int32_t capacity, int64_t *active,
+                                        int64_t *gathered, int64_t *ret,
+                                        int64_t *scattered, int32_t *rounds);
+GAS_API gas_status gas_core_last_run_ms(gas_core *c, float *ms);
+GAS_API gas_status gas_core_save_vertex_data(gas_core *c);
+GAS_API gas_status gas_core_restore_vertex_data(gas_core *c);
+GAS_API gas_status gas_core_set_profiling(gas_core *c, int32_t enabled);
+GAS_API gas_status gas_core_kernel_times(gas_core *c, float *gatherMs, float *scatterMs,
+                                         int32_t *gatherLaunches, int32_t *scatterLaunches);
+/* Waits for queued work and reports device-side errors. */
+GAS_API gas_status gas_core_sync(gas_core *c);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

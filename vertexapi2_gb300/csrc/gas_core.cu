@@ -1,0 +1,792 @@
+// Core layer of the GB300 GAS engine (gas_gb300_core.h): device graph
+// layout, frontier state, scatter/activate launches and the iteration loop.
+//
+// HBM layout per graph (int32 ids, as the reference's Int = int32_t):
+//   inOffsets[V+1]  inSources[E]   CSC, gather side   (gpugas.h:100-103)
+//   outOffsets[V+1] outDests[E]    CSR, scatter side  (gpugas.h:105-108)
+//   edgeData[E]                    CSC order          (gpugas.h:259-263)
+//   vertexData[V], vertexNew[V]    apply writes vertexNew, scatter commits
+//   front{Vid,Pre}[2][V]           frontier lists (ids + in-degree prefix)
+//   scat{Vid,Pre}[2][V]            vertices whose apply returned true
+//   split arrays                   merge-path tile splits written by the
+//                                  producer of each list
+//   mark[V]                        round stamp of the last activation
+//   carry{Val,Flag}[tiles]         published tile aggregates (look-back)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gas_gb300_core.h"
+#include "gas_gb300/detail/scatter.cuh"
+#include "gas_internal.h"
+
+using gas::detail::ScatterArgs;
+
+namespace gas {
+namespace internal {
+
+thread_local std::string g_last_error;
+
+gas_status fail(gas_status code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+gas_status cuda_fail(cudaError_t e, const char *what) {
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return fail(GAS_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  }
+  return fail(GAS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Stable counting sort of an edge list by `key` into offsets/adjacency
+// (util.h:79-121 semantics; ties keep edge-list order).  perm[p] = edge
+// index placed at position p.
+void build_adjacency(int32_t nV, int32_t nE, const int32_t *key, const int32_t *other,
+                     std::vector<int32_t> &off, std::vector<int32_t> &adj,
+                     std::vector<int32_t> *perm) {
+  off.assign((size_t)nV + 1, 0);
+  for (int32_t i = 0; i < nE; ++i) off[(size_t)key[i] + 1]++;
+  for (int32_t v = 0; v < nV; ++v) off[(size_t)v + 1] += off[v];
+  std::vector<int32_t> cur(off.begin(), off.end() - 1);
+  adj.resize((size_t)std::max(nE, 1));
+  if (perm) perm->resize((size_t)std::max(nE, 1));
+  for (int32_t i = 0; i < nE; ++i) {
+    const int32_t p = cur[key[i]]++;
+    adj[p] = other[i];
+    if (perm) (*perm)[p] = i;
+  }
+}
+
+}  // namespace internal
+}  // namespace gas
+
+using namespace gas::internal;
+
+namespace {
+
+struct Ctl {
+  unsigned long long fcnt[2];
+  unsigned long long scnt[2];
+  unsigned tile[2];
+  unsigned err;
+  unsigned pad;
+};
+
+enum DirtyBit : unsigned {
+  kF0 = 1u, kF1 = 2u, kS0 = 4u, kS1 = 8u, kT0 = 16u, kT1 = 32u,
+};
+
+constexpr int kRing = 8;
+constexpr int kLag = 3;
+constexpr int kMaxRounds = 1 << 16;
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count) {
+  return cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(count, 1));
+}
+
+}  // namespace
+
+struct gas_core_s {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int numSMs = 0;
+  int scatterGrid = 0;
+  // graph
+  bool haveGraph = false;
+  int32_t nV = 0, nE = 0;
+  int32_t edgeBytes = 0, vertexBytes = 0, gatherBytes = 0;
+  std::vector<int32_t> hInOff, hOutOff, cscPerm;
+  int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
+  void *ed = nullptr;
+  void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr;
+  int32_t *fvid[2] = {nullptr, nullptr}, *fpre[2] = {nullptr, nullptr};
+  int32_t *fsplit[2] = {nullptr, nullptr}, *rsplit = nullptr;
+  int32_t *svid[2] = {nullptr, nullptr}, *spre[2] = {nullptr, nullptr};
+  int32_t *ssplit[2] = {nullptr, nullptr};
+  int32_t *mark = nullptr;
+  void *carryVal = nullptr;
+  unsigned *carryFlag = nullptr;
+  Ctl *ctl = nullptr;
+  unsigned long long *stats = nullptr;
+  int32_t maxGatherTiles = 0, maxScatTiles = 0;
+  // protocol state
+  int cur = 0, sidx = 0;
+  bool rangeMode = true;
+  int32_t rstart = 0, rcount = 0;
+  bool pendingCommit = false;
+  bool haveScatList = false;
+  bool countValid = false;
+  int32_t countCache = 0;
+  unsigned dirty = 0;
+  unsigned epoch = 0;
+  int32_t stamp = 0;
+  int32_t iteration = 0;
+  int32_t round = 0;
+  // run bookkeeping
+  unsigned long long *pinned = nullptr;
+  cudaEvent_t ev[kRing] = {};
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  float lastMs = 0.f;
+  // optional per-kernel profile of run()
+  bool profiling = false;
+  std::vector<cudaEvent_t> pev;  // 4 per round: gather start/end, scatter start/end
+  float gatherMs = 0.f, scatterMs = 0.f;
+  int32_t gatherLaunches = 0, scatterLaunches = 0;
+};
+
+namespace {
+
+void free_graph(gas_core *c) {
+  void *ptrs[] = {c->inOff, c->inSrc, c->outOff, c->outDst, c->ed, c->vd, c->vnew, c->vsaved,
+                  c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
+                  c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
+                  c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
+  c->ed = c->vd = c->vnew = c->vsaved = nullptr;
+  for (int k = 0; k < 2; ++k) {
+    c->fvid[k] = c->fpre[k] = c->fsplit[k] = nullptr;
+    c->svid[k] = c->spre[k] = c->ssplit[k] = nullptr;
+  }
+  c->rsplit = nullptr;
+  c->mark = nullptr;
+  c->carryVal = nullptr;
+  c->carryFlag = nullptr;
+  c->ctl = nullptr;
+  c->stats = nullptr;
+  c->haveGraph = false;
+}
+
+gas_status set_device(gas_core *c) {
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  return GAS_OK;
+}
+
+gas_status clean(gas_core *c, unsigned need) {
+  unsigned d = c->dirty & need;
+  if (!d) return GAS_OK;
+  struct {
+    unsigned bit;
+    void *ptr;
+    size_t bytes;
+  } m[] = {{kF0, &c->ctl->fcnt[0], 8}, {kF1, &c->ctl->fcnt[1], 8},
+           {kS0, &c->ctl->scnt[0], 8}, {kS1, &c->ctl->scnt[1], 8},
+           {kT0, &c->ctl->tile[0], 4}, {kT1, &c->ctl->tile[1], 4}};
+  for (auto &x : m)
+    if (d & x.bit) {
+      cudaError_t e = cudaMemsetAsync(x.ptr, 0, x.bytes, c->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    }
+  c->dirty &= ~d;
+  return GAS_OK;
+}
+
+unsigned fbit(int k) { return k ? kF1 : kF0; }
+unsigned sbit(int k) { return k ? kS1 : kS0; }
+
+gas_status check_device_error(gas_core *c) {
+  unsigned err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, &c->ctl->err, sizeof(err), cudaMemcpyDeviceToHost,
+                                  c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "device sync");
+  if (err) {
+    cudaMemsetAsync(&c->ctl->err, 0, sizeof(unsigned), c->stream);
+    if (err & GAS_DEVERR_TIMEOUT)
+      return fail(GAS_ERR_TIMEOUT, "a bounded device wait (tile look-back) timed out");
+    return fail(GAS_ERR_STATE, "device list capacity exceeded (error bits 0x%x)", err);
+  }
+  return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gas_status gas_core_create(int32_t device, void *stream, gas_core **out) {
+  if (!out) return fail(GAS_ERR_INVALID, "gas_core_create: out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return fail(GAS_ERR_NO_DEVICE, "no CUDA device %d", device);
+  }
+  gas_core *c = new (std::nothrow) gas_core_s();
+  if (!c) return fail(GAS_ERR_OOM, "host allocation");
+  c->device = device;
+  c->stream = (cudaStream_t)stream;
+  if (set_device(c) != GAS_OK) {
+    delete c;
+    return GAS_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gas::detail::scatter_activate_kernel,
+                                                gas::detail::kSNT, 0);
+  c->scatterGrid = std::max(1, per) * std::max(1, c->numSMs);
+  e = cudaMallocHost((void **)&c->pinned, sizeof(unsigned long long) * kRing);
+  if (e != cudaSuccess) {
+    delete c;
+    return cuda_fail(e, "cudaMallocHost");
+  }
+  for (int k = 0; k < kRing; ++k) cudaEventCreateWithFlags(&c->ev[k], cudaEventDisableTiming);
+  cudaEventCreate(&c->t0);
+  cudaEventCreate(&c->t1);
+  *out = c;
+  return GAS_OK;
+}
+
+gas_status gas_core_destroy(gas_core *c) {
+  if (!c) return GAS_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_graph(c);
+  for (int k = 0; k < kRing; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (cudaEvent_t ev : c->pev) cudaEventDestroy(ev);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  delete c;
+  return GAS_OK;
+}
+
+gas_status gas_core_stream(gas_core *c, void **stream) {
+  if (!c || !stream) return fail(GAS_ERR_INVALID, "gas_core_stream: null argument");
+  *stream = (void *)c->stream;
+  return GAS_OK;
+}
+
+gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t *srcs,
+                              const int32_t *dsts, const void *edgeData, int32_t edgeBytes,
+                              int32_t vertexBytes, int32_t gatherBytes) {
+  if (!c) return fail(GAS_ERR_INVALID, "gas_core_set_graph: engine is NULL");
+  if (nV < 0 || nE < 0) return fail(GAS_ERR_INVALID, "negative vertex or edge count");
+  if (nE > 0 && (!srcs || !dsts)) return fail(GAS_ERR_INVALID, "edge list is NULL");
+  if (edgeBytes < 0 || vertexBytes <= 0 || gatherBytes <= 0)
+    return fail(GAS_ERR_INVALID, "bad element sizes");
+  if (edgeBytes > 0 && nE > 0 && !edgeData)
+    return fail(GAS_ERR_INVALID, "edge data is NULL but EdgeData is not empty");
+  if ((long long)nV + nE + 2LL * GAS_GATHER_TILE >= (1LL << 31))
+    return fail(GAS_ERR_UNSUPPORTED, "vertices + edges must stay below 2^31 (int32 ids)");
+  for (int32_t i = 0; i < nE; ++i)
+    if ((unsigned)srcs[i] >= (unsigned)nV || (unsigned)dsts[i] >= (unsigned)nV)
+      return fail(GAS_ERR_INVALID, "edge %d (%d -> %d) has a vertex id outside [0, %d)", i,
+                  srcs[i], dsts[i], nV);
+  gas_status st = set_device(c);
+  if (st) return st;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_graph(c);
+
+  // host CSC (gather) and CSR (scatter), both stable in edge-list order
+  std::vector<int32_t> inSrcH, outDstH;
+  std::vector<int32_t> *perm = edgeBytes > 0 ? &c->cscPerm : nullptr;
+  std::thread tcsr([&] { build_adjacency(nV, nE, srcs, dsts, c->hOutOff, outDstH, nullptr); });
+  build_adjacency(nV, nE, dsts, srcs, c->hInOff, inSrcH, perm);
+  tcsr.join();
+  if (!perm) c->cscPerm.clear();
+
+  c->nV = nV;
+  c->nE = nE;
+  c->edgeBytes = edgeBytes;
+  c->vertexBytes = vertexBytes;
+  c->gatherBytes = gatherBytes;
+  c->maxGatherTiles = (int32_t)(((long long)nV + nE) / GAS_GATHER_TILE + 2);
+  c->maxScatTiles = (int32_t)(((long long)nV + nE) / GAS_SCATTER_TILE + 2);
+
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  A(dalloc(&c->inOff, (size_t)nV + 1));
+  A(dalloc(&c->inSrc, (size_t)nE));
+  A(dalloc(&c->outOff, (size_t)nV + 1));
+  A(dalloc(&c->outDst, (size_t)nE));
+  if (edgeBytes > 0) A(cudaMalloc(&c->ed, (size_t)edgeBytes * std::max(nE, 1)));
+  A(cudaMalloc(&c->vd, (size_t)vertexBytes * std::max(nV, 1)));
+  A(cudaMalloc(&c->vnew, (size_t)vertexBytes * std::max(nV, 1)));
+  for (int k = 0; k < 2; ++k) {
+    A(dalloc(&c->fvid[k], (size_t)nV));
+    A(dalloc(&c->fpre[k], (size_t)nV));
+    A(dalloc(&c->fsplit[k], (size_t)c->maxGatherTiles));
+    A(dalloc(&c->svid[k], (size_t)nV));
+    A(dalloc(&c->spre[k], (size_t)nV));
+    A(dalloc(&c->ssplit[k], (size_t)c->maxScatTiles));
+  }
+  A(dalloc(&c->rsplit, (size_t)c->maxGatherTiles));
+  A(dalloc(&c->mark, (size_t)nV));
+  const size_t gb = (size_t)((gatherBytes + 15) / 16 * 16);
+  A(cudaMalloc(&c->carryVal, gb * c->maxGatherTiles));
+  A(dalloc(&c->carryFlag, (size_t)c->maxGatherTiles));
+  A(dalloc(&c->ctl, 1));
+  A(dalloc(&c->stats, (size_t)kMaxRounds * 2));
+  if (e != cudaSuccess) {
+    free_graph(c);
+    return cuda_fail(e, "setGraph device allocation");
+  }
+  A(cudaMemcpyAsync(c->inOff, c->hInOff.data(), sizeof(int32_t) * ((size_t)nV + 1),
+                    cudaMemcpyHostToDevice, c->stream));
+  A(cudaMemcpyAsync(c->outOff, c->hOutOff.data(), sizeof(int32_t) * ((size_t)nV + 1),
+                    cudaMemcpyHostToDevice, c->stream));
+  if (nE > 0) {
+    A(cudaMemcpyAsync(c->inSrc, inSrcH.data(), sizeof(int32_t) * nE, cudaMemcpyHostToDevice,
+                      c->stream));
+    A(cudaMemcpyAsync(c->outDst, outDstH.data(), sizeof(int32_t) * nE, cudaMemcpyHostToDevice,
+                      c->stream));
+  }
+  std::vector<char> edSorted;
+  if (edgeBytes > 0 && nE > 0) {
+    edSorted.resize((size_t)edgeBytes * nE);
+    const char *src = reinterpret_cast<const char *>(edgeData);
+    for (int32_t p = 0; p < nE; ++p)
+      memcpy(&edSorted[(size_t)p * edgeBytes], src + (size_t)c->cscPerm[p] * edgeBytes,
+             edgeBytes);
+    A(cudaMemcpyAsync(c->ed, edSorted.data(), edSorted.size(), cudaMemcpyHostToDevice,
+                      c->stream));
+  }
+  A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
+  A(cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream));
+  A(cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream));
+  A(cudaMemsetAsync(c->vd, 0, (size_t)vertexBytes * std::max(nV, 1), c->stream));
+  A(cudaStreamSynchronize(c->stream));  // host staging buffers die here
+  if (e != cudaSuccess) {
+    free_graph(c);
+    return cuda_fail(e, "setGraph upload");
+  }
+  c->haveGraph = true;
+  c->dirty = 0;
+  c->epoch = 0;
+  c->stamp = 0;
+  c->iteration = 0;
+  c->round = 0;
+  c->rangeMode = true;
+  c->rstart = 0;
+  c->rcount = 0;
+  c->cur = c->sidx = 0;
+  c->pendingCommit = false;
+  c->haveScatList = false;
+  return GAS_OK;
+}
+
+gas_status gas_core_upload_vertex_data(gas_core *c, const void *host) {
+  if (!c || !host) return fail(GAS_ERR_INVALID, "upload_vertex_data: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (c->nV == 0) return GAS_OK;
+  cudaError_t e = cudaMemcpyAsync(c->vd, host, (size_t)c->vertexBytes * c->nV,
+                                  cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "vertex data upload");
+}
+
+gas_status gas_core_download_vertex_data(gas_core *c, void *host) {
+  if (!c || !host) return fail(GAS_ERR_INVALID, "download_vertex_data: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  gas_status st = check_device_error(c);
+  if (st) return st;
+  if (c->nV == 0) return GAS_OK;
+  cudaError_t e = cudaMemcpyAsync(host, c->vd, (size_t)c->vertexBytes * c->nV,
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "vertex data download");
+}
+
+gas_status gas_core_download_edge_data(gas_core *c, void *host) {
+  if (!c || !host) return fail(GAS_ERR_INVALID, "download_edge_data: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (c->edgeBytes == 0 || c->nE == 0) return GAS_OK;
+  std::vector<char> tmp((size_t)c->edgeBytes * c->nE);
+  cudaError_t e = cudaMemcpyAsync(tmp.data(), c->ed, tmp.size(), cudaMemcpyDeviceToHost,
+                                  c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "edge data download");
+  char *dst = reinterpret_cast<char *>(host);
+  for (int32_t p = 0; p < c->nE; ++p)
+    memcpy(dst + (size_t)c->cscPerm[p] * c->edgeBytes, &tmp[(size_t)p * c->edgeBytes],
+           c->edgeBytes);
+  return GAS_OK;
+}
+
+gas_status gas_core_vertex_data(gas_core *c, void **dev) {
+  if (!c || !dev) return fail(GAS_ERR_INVALID, "vertex_data: null argument");
+  *dev = c->vd;
+  return GAS_OK;
+}
+
+gas_status gas_core_set_active(gas_core *c, int32_t start, int32_t end) {
+  if (!c) return fail(GAS_ERR_INVALID, "set_active: engine is NULL");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (start < 0 || end < start || end > c->nV)
+    return fail(GAS_ERR_INVALID, "active range [%d, %d) outside [0, %d]", start, end, c->nV);
+  gas_status st = set_device(c);
+  if (st) return st;
+  cudaError_t e = cudaMemsetAsync(c->ctl, 0, sizeof(Ctl) - 8, c->stream);  // keep err
+  if (e != cudaSuccess) return cuda_fail(e, "set_active reset");
+  c->dirty = 0;
+  c->rangeMode = true;
+  c->rstart = start;
+  c->rcount = end - start;
+  c->cur = c->sidx = 0;
+  c->pendingCommit = false;
+  c->haveScatList = false;
+  c->countValid = false;
+  c->round = 0;
+  const int32_t T = c->hInOff[end] - c->hInOff[start];
+  const long long items = (long long)c->rcount + T;
+  const int nsplit = (int)((items + GAS_GATHER_TILE - 1) / GAS_GATHER_TILE) + 1;
+  if (c->rcount > 0) {
+    gas::detail::range_split_kernel<<<(nsplit + 127) / 128, 128, 0, c->stream>>>(
+        c->inOff, start, c->rcount, T, c->rsplit, nsplit);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "range split launch");
+  }
+  return GAS_OK;
+}
+
+gas_status gas_core_count_active(gas_core *c, int32_t *n) {
+  if (!c || !n) return fail(GAS_ERR_INVALID, "count_active: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (c->rangeMode) {
+    *n = c->rcount;
+    return GAS_OK;
+  }
+  if (c->countValid) {
+    *n = c->countCache;
+    return GAS_OK;
+  }
+  gas_status st = check_device_error(c);
+  if (st) return st;
+  unsigned long long v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, &c->ctl->fcnt[c->cur], 8, cudaMemcpyDeviceToHost,
+                                  c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "count_active");
+  *n = (int32_t)std::min<unsigned long long>(v >> 32, (unsigned long long)c->nV);
+  c->countCache = *n;
+  c->countValid = true;
+  return GAS_OK;
+}
+
+gas_status gas_core_set_iteration(gas_core *c, int32_t iteration) {
+  if (!c) return fail(GAS_ERR_INVALID, "set_iteration: engine is NULL");
+  c->iteration = iteration;
+  return GAS_OK;
+}
+
+gas_status gas_core_gather_apply(gas_core *c, int32_t haveGather, gas_gather_launch_fn launch,
+                                 void *user) {
+  if (!c || !launch) return fail(GAS_ERR_INVALID, "gather_apply: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  gas_status st = set_device(c);
+  if (st) return st;
+  st = clean(c, sbit(c->sidx) | kT0);
+  if (st) return st;
+  if (++c->epoch == 0xffffffffu) {
+    cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream);
+    c->epoch = 1;
+  }
+  gas_gather_args a;
+  memset(&a, 0, sizeof(a));
+  a.nVertices = c->nV;
+  a.nEdges = c->nE;
+  a.inOffsets = c->inOff;
+  a.inSources = c->inSrc;
+  a.outOffsets = c->outOff;
+  a.edgeData = c->ed;
+  a.vertexData = c->vd;
+  a.vertexNew = c->vnew;
+  a.rangeMode = c->rangeMode ? 1 : 0;
+  a.rangeStart = c->rstart;
+  a.rangeCount = c->rcount;
+  a.rangeBase = c->rangeMode ? c->hInOff[c->rstart] : 0;
+  a.frontVid = c->fvid[c->cur];
+  a.frontPre = c->fpre[c->cur];
+  a.frontCount = &c->ctl->fcnt[c->cur];
+  a.frontSplit = c->rangeMode ? c->rsplit : c->fsplit[c->cur];
+  a.scatVid = c->svid[c->sidx];
+  a.scatPre = c->spre[c->sidx];
+  a.scatSplit = c->ssplit[c->sidx];
+  a.scatCount = &c->ctl->scnt[c->sidx];
+  a.capacity = c->nV;
+  a.maxScatTiles = c->maxScatTiles;
+  a.resetCount = &c->ctl->fcnt[c->cur ^ 1];
+  a.resetTile = &c->ctl->tile[1];
+  a.tileCounter = &c->ctl->tile[0];
+  a.carryVal = c->carryVal;
+  a.carryFlag = c->carryFlag;
+  a.epoch = c->epoch;
+  a.errWord = &c->ctl->err;
+  a.statSlot = c->round < kMaxRounds ? c->stats + 2 * (size_t)c->round : nullptr;
+  a.iteration = c->iteration;
+  a.haveGather = haveGather ? 1 : 0;
+  st = launch(user, &a, (void *)c->stream);
+  if (st) return st;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "gather/apply launch");
+  c->dirty |= sbit(c->sidx) | kT0;
+  c->dirty &= ~(fbit(c->cur ^ 1) | kT1);
+  c->pendingCommit = haveGather != 0;
+  c->haveScatList = true;
+  return GAS_OK;
+}
+
+gas_status gas_core_scatter_activate(gas_core *c) {
+  if (!c) return fail(GAS_ERR_INVALID, "scatter_activate: engine is NULL");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (!c->haveScatList) return fail(GAS_ERR_STATE, "scatterActivate needs a gatherApply first");
+  gas_status st = set_device(c);
+  if (st) return st;
+  st = clean(c, fbit(c->cur ^ 1) | kT1);
+  if (st) return st;
+  if (++c->stamp == 0x7fffffff) {
+    cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream);
+    c->stamp = 1;
+  }
+  ScatterArgs a;
+  memset(&a, 0, sizeof(a));
+  a.outOffsets = c->outOff;
+  a.outDests = c->outDst;
+  a.inOffsets = c->inOff;
+  a.scatVid = c->svid[c->sidx];
+  a.scatPre = c->spre[c->sidx];
+  a.scatSplit = c->ssplit[c->sidx];
+  a.scatCount = &c->ctl->scnt[c->sidx];
+  a.commit = c->pendingCommit ? 1 : 0;
+  a.vertexBytes = c->vertexBytes;
+  a.vertexData = c->vd;
+  a.vertexNew = c->vnew;
+  a.rangeMode = c->rangeMode ? 1 : 0;
+  a.rangeStart = c->rstart;
+  a.rangeCount = c->rcount;
+  a.frontVid = c->fvid[c->cur];
+  a.frontCount = &c->ctl->fcnt[c->cur];
+  a.nextVid = c->fvid[c->cur ^ 1];
+  a.nextPre = c->fpre[c->cur ^ 1];
+  a.nextSplit = c->fsplit[c->cur ^ 1];
+  a.nextCount = &c->ctl->fcnt[c->cur ^ 1];
+  a.maxGatherTiles = c->maxGatherTiles;
+  a.capacity = c->nV;
+  a.mark = c->mark;
+  a.stamp = c->stamp;
+  a.tileCounter = &c->ctl->tile[1];
+  a.resetTile = &c->ctl->tile[0];
+  a.resetScatCount = &c->ctl->scnt[c->sidx ^ 1];
+  a.errWord = &c->ctl->err;
+  a.statSlot = c->round < kMaxRounds ? c->stats + 2 * (size_t)c->round : nullptr;
+  gas::detail::scatter_activate_kernel<<<c->scatterGrid, gas::detail::kSNT, 0, c->stream>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "scatter launch");
+  c->dirty |= fbit(c->cur ^ 1) | kT1;
+  c->dirty &= ~(kT0 | sbit(c->sidx ^ 1));
+  c->pendingCommit = false;
+  c->haveScatList = false;
+  c->countValid = false;
+  ++c->round;
+  return GAS_OK;
+}
+
+gas_status gas_core_next_iter(gas_core *c) {
+  if (!c) return fail(GAS_ERR_INVALID, "next_iter: engine is NULL");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  c->cur ^= 1;
+  c->sidx ^= 1;
+  c->rangeMode = false;
+  c->countValid = false;
+  return GAS_OK;
+}
+
+gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
+                        gas_gather_launch_fn launch, void *user, int32_t *iterations) {
+  if (!c || !launch) return fail(GAS_ERR_INVALID, "run: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  gas_status st = set_device(c);
+  if (st) return st;
+  if (iterations) *iterations = 0;
+  int32_t n0 = 0;
+  st = gas_core_count_active(c, &n0);
+  if (st) return st;
+  cudaEventRecord(c->t0, c->stream);
+  const int32_t base = c->iteration;
+  int32_t done = -1, launched = 0;
+  if (n0 == 0) done = 0;
+  for (int32_t r = 0; done < 0 && (maxIters <= 0 || r < maxIters); ++r) {
+    c->iteration = base + r;
+    cudaEvent_t *pe = nullptr;
+    if (c->profiling) {
+      while (c->pev.size() < 4 * (size_t)(r + 1)) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "event");
+        c->pev.push_back(ev);
+      }
+      pe = &c->pev[4 * (size_t)r];
+      cudaEventRecord(pe[0], c->stream);
+    }
+    if ((st = gas_core_gather_apply(c, haveGather, launch, user))) return st;
+    if (pe) {
+      cudaEventRecord(pe[1], c->stream);
+      cudaEventRecord(pe[2], c->stream);
+    }
+    if ((st = gas_core_scatter_activate(c))) return st;
+    if (pe) cudaEventRecord(pe[3], c->stream);
+    if ((st = gas_core_next_iter(c))) return st;
+    cudaError_t e = cudaMemcpyAsync(&c->pinned[r % kRing], &c->ctl->fcnt[c->cur], 8,
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev[r % kRing], c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "run bookkeeping");
+    launched = r + 1;
+    if (r >= kLag) {
+      const int k = r - kLag;
+      cudaEventSynchronize(c->ev[k % kRing]);
+      if ((c->pinned[k % kRing] >> 32) == 0) done = k + 1;
+    }
+  }
+  cudaEventRecord(c->t1, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "run");
+  if (done < 0) {
+    done = launched;
+    for (int k = std::max(0, launched - kLag - 1); k < launched; ++k)
+      if ((c->pinned[k % kRing] >> 32) == 0) {
+        done = k + 1;
+        break;
+      }
+  }
+  c->iteration = base + done;
+  cudaEventElapsedTime(&c->lastMs, c->t0, c->t1);
+  c->gatherMs = c->scatterMs = 0.f;
+  c->gatherLaunches = c->scatterLaunches = 0;
+  if (c->profiling) {
+    for (int32_t r = 0; r < launched; ++r) {
+      float g = 0.f, sc = 0.f;
+      cudaEventElapsedTime(&g, c->pev[4 * (size_t)r], c->pev[4 * (size_t)r + 1]);
+      cudaEventElapsedTime(&sc, c->pev[4 * (size_t)r + 2], c->pev[4 * (size_t)r + 3]);
+      c->gatherMs += g;
+      c->scatterMs += sc;
+    }
+    c->gatherLaunches = c->scatterLaunches = launched;
+  }
+  if (iterations) *iterations = done;
+  return check_device_error(c);
+}
+
+gas_status gas_core_round_stats(gas_core *c, int32_t capacity, int64_t *active,
+                                int64_t *gathered, int64_t *ret, int64_t *scattered,
+                                int32_t *rounds) {
+  if (!c) return fail(GAS_ERR_INVALID, "round_stats: engine is NULL");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  const int nr = std::min(c->round, kMaxRounds);
+  if (rounds) *rounds = nr;
+  const int m = std::min(nr, std::max(capacity, 0));
+  if (m == 0) return GAS_OK;
+  std::vector<unsigned long long> h((size_t)m * 2);
+  cudaError_t e = cudaMemcpyAsync(h.data(), c->stats, h.size() * 8, cudaMemcpyDeviceToHost,
+                                  c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "round_stats");
+  for (int k = 0; k < m; ++k) {
+    if (active) active[k] = (int64_t)(h[2 * k] >> 32);
+    if (gathered) gathered[k] = (int64_t)(h[2 * k] & 0xffffffffull);
+    if (ret) ret[k] = (int64_t)(h[2 * k + 1] >> 32);
+    if (scattered) scattered[k] = (int64_t)(h[2 * k + 1] & 0xffffffffull);
+  }
+  return GAS_OK;
+}
+
+gas_status gas_core_last_run_ms(gas_core *c, float *ms) {
+  if (!c || !ms) return fail(GAS_ERR_INVALID, "last_run_ms: null argument");
+  *ms = c->lastMs;
+  return GAS_OK;
+}
+
+gas_status gas_core_save_vertex_data(gas_core *c) {
+  if (!c) return fail(GAS_ERR_INVALID, "save_vertex_data: engine is NULL");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  gas_status st = set_device(c);
+  if (st) return st;
+  const size_t bytes = (size_t)c->vertexBytes * std::max(c->nV, 1);
+  if (!c->vsaved) {
+    cudaError_t e = cudaMalloc(&c->vsaved, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "save_vertex_data allocation");
+  }
+  cudaError_t e = cudaMemcpyAsync(c->vsaved, c->vd, bytes, cudaMemcpyDeviceToDevice, c->stream);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "save_vertex_data");
+}
+
+gas_status gas_core_restore_vertex_data(gas_core *c) {
+  if (!c) return fail(GAS_ERR_INVALID, "restore_vertex_data: engine is NULL");
+  if (!c->haveGraph || !c->vsaved) return fail(GAS_ERR_STATE, "no saved vertex data");
+  gas_status st = set_device(c);
+  if (st) return st;
+  const size_t bytes = (size_t)c->vertexBytes * std::max(c->nV, 1);
+  cudaError_t e = cudaMemcpyAsync(c->vd, c->vsaved, bytes, cudaMemcpyDeviceToDevice, c->stream);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "restore_vertex_data");
+}
+
+gas_status gas_core_set_profiling(gas_core *c, int32_t enabled) {
+  if (!c) return fail(GAS_ERR_INVALID, "set_profiling: engine is NULL");
+  c->profiling = enabled != 0;
+  return GAS_OK;
+}
+
+gas_status gas_core_kernel_times(gas_core *c, float *gatherMs, float *scatterMs,
+                                 int32_t *gatherLaunches, int32_t *scatterLaunches) {
+  if (!c) return fail(GAS_ERR_INVALID, "kernel_times: engine is NULL");
+  if (gatherMs) *gatherMs = c->gatherMs;
+  if (scatterMs) *scatterMs = c->scatterMs;
+  if (gatherLaunches) *gatherLaunches = c->gatherLaunches;
+  if (scatterLaunches) *scatterLaunches = c->scatterLaunches;
+  return GAS_OK;
+}
+
+gas_status gas_core_sync(gas_core *c) {
+  if (!c) return fail(GAS_ERR_INVALID, "sync: engine is NULL");
+  if (!c->haveGraph) return GAS_OK;
+  return check_device_error(c);
+}
+
+const char *gas_status_string(gas_status s) {
+  switch (s) {
+    case GAS_OK: return "ok";
+    case GAS_ERR_INVALID: return "invalid argument";
+    case GAS_ERR_OOM: return "out of memory";
+    case GAS_ERR_CUDA: return "CUDA error";
+    case GAS_ERR_TIMEOUT: return "device wait timed out";
+    case GAS_ERR_STATE: return "invalid state";
+    case GAS_ERR_UNSUPPORTED: return "unsupported";
+    case GAS_ERR_NO_DEVICE: return "no supported device";
+    default: return "unknown status";
+  }
+}
+
+const char *gas_last_error(void) { return g_last_error.c_str(); }
+
+int32_t gas_device_supported(int32_t device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return 0;
+  }
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+  return (major == 10 && minor == 3) ? 1 : 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,147 @@
+"""Python mirror of vertexAPI2's GASEngineGPU over the C ABI.
+
+Method names and meaning follow gpugas.h:212-772 (setGraph, getResults,
+setActive, countActive, gatherApply, scatterActivate, nextIter, run) for
+the built-in programs; every call goes through libgas_gb300.so's
+gas_engine_* entry points and raises GasError on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, load
+from .programs import EDGE_DTYPES, VERTEX_DTYPES
+
+
+def _i32ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class GASEngine:
+    def __init__(self, program: int, device: int = 0, stream: int | None = None):
+        self.program = program
+        self._lib = load()
+        h = C.c_void_p()
+        check(self._lib.gas_engine_create(program, device, C.c_void_p(stream or 0), C.byref(h)),
+              "gas_engine_create")
+        self._h = h
+        self._keep: list = []
+        self.vertex_data: np.ndarray | None = None
+        self.edge_data: np.ndarray | None = None
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gas_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # gpugas.h:212-322.  vertex_data / edge_data are borrowed (kept alive
+    # here) and written back by get_results, as in the reference.
+    def set_graph(self, n_vertices: int, vertex_data: np.ndarray | None, srcs: np.ndarray,
+                  dsts: np.ndarray, edge_data: np.ndarray | None = None) -> None:
+        srcs = np.ascontiguousarray(srcs, dtype=np.int32)
+        dsts = np.ascontiguousarray(dsts, dtype=np.int32)
+        if vertex_data is not None:
+            want = VERTEX_DTYPES[self.program]
+            if vertex_data.dtype != want or not vertex_data.flags.c_contiguous:
+                raise TypeError(f"vertex data must be contiguous {want}")
+        if edge_data is not None:
+            want = EDGE_DTYPES.get(self.program)
+            if want is None:
+                edge_data = None
+            elif edge_data.dtype != want or not edge_data.flags.c_contiguous:
+                raise TypeError(f"edge data must be contiguous {want}")
+        self.vertex_data, self.edge_data = vertex_data, edge_data
+        self._keep = [srcs, dsts]
+        vd = vertex_data.ctypes.data_as(C.c_void_p) if vertex_data is not None else None
+        ed = edge_data.ctypes.data_as(C.c_void_p) if edge_data is not None else None
+        check(self._lib.gas_engine_set_graph(self._h, n_vertices, vd, int(srcs.shape[0]), ed,
+                                             _i32ptr(srcs), _i32ptr(dsts)), "gas_engine_set_graph")
+
+    def set_vertex_data(self, host: np.ndarray) -> None:
+        check(self._lib.gas_engine_set_vertex_data(self._h, host.ctypes.data_as(C.c_void_p)),
+              "gas_engine_set_vertex_data")
+
+    def get_results(self) -> None:
+        check(self._lib.gas_engine_get_results(self._h), "gas_engine_get_results")
+
+    def set_active(self, start: int, end: int) -> None:
+        check(self._lib.gas_engine_set_active(self._h, start, end), "gas_engine_set_active")
+
+    def count_active(self) -> int:
+        n = C.c_int32()
+        check(self._lib.gas_engine_count_active(self._h, C.byref(n)), "gas_engine_count_active")
+        return n.value
+
+    def gather_apply(self, have_gather: bool = True) -> None:
+        check(self._lib.gas_engine_gather_apply(self._h, int(have_gather)), "gas_engine_gather_apply")
+
+    def scatter_activate(self, have_scatter: bool = True) -> None:
+        check(self._lib.gas_engine_scatter_activate(self._h, int(have_scatter)),
+              "gas_engine_scatter_activate")
+
+    def next_iter(self, wait: bool = True) -> int | None:
+        n = C.c_int32()
+        check(self._lib.gas_engine_next_iter(self._h, C.byref(n) if wait else None),
+              "gas_engine_next_iter")
+        return n.value if wait else None
+
+    def run(self, max_iters: int = 0) -> int:
+        it = C.c_int32()
+        check(self._lib.gas_engine_run(self._h, max_iters, C.byref(it)), "gas_engine_run")
+        return it.value
+
+    def set_iteration(self, iteration: int) -> None:
+        check(self._lib.gas_engine_set_iteration(self._h, iteration), "gas_engine_set_iteration")
+
+    def round_stats(self, capacity: int = 1 << 16) -> dict[str, np.ndarray]:
+        arrs = {k: np.zeros(capacity, dtype=np.int64)
+                for k in ("active", "gathered", "ret", "scattered")}
+        rounds = C.c_int32()
+        p = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))
+        check(self._lib.gas_engine_round_stats(self._h, capacity, p(arrs["active"]),
+                                               p(arrs["gathered"]), p(arrs["ret"]),
+                                               p(arrs["scattered"]), C.byref(rounds)),
+              "gas_engine_round_stats")
+        r = min(rounds.value, capacity)
+        return {k: v[:r] for k, v in arrs.items()}
+
+    def save_vertex_data(self) -> None:
+        check(self._lib.gas_engine_save_vertex_data(self._h), "gas_engine_save_vertex_data")
+
+    def restore_vertex_data(self) -> None:
+        check(self._lib.gas_engine_restore_vertex_data(self._h), "gas_engine_restore_vertex_data")
+
+    def set_profiling(self, enabled: bool) -> None:
+        check(self._lib.gas_engine_set_profiling(self._h, int(enabled)), "gas_engine_set_profiling")
+
+    def kernel_times(self) -> dict:
+        g, s = C.c_float(), C.c_float()
+        gl, sl = C.c_int32(), C.c_int32()
+        check(self._lib.gas_engine_kernel_times(self._h, C.byref(g), C.byref(s), C.byref(gl),
+                                                C.byref(sl)), "gas_engine_kernel_times")
+        return {"gather_ms": g.value, "scatter_ms": s.value, "gather_launches": gl.value,
+                "scatter_launches": sl.value}
+
+    def last_run_ms(self) -> float:
+        ms = C.c_float()
+        check(self._lib.gas_engine_last_run_ms(self._h, C.byref(ms)), "gas_engine_last_run_ms")
+        return float(ms.value)
+
+
+def device_supported(device: int = 0) -> bool:
+    return bool(load().gas_device_supported(device))
