@@ -79,7 +79,20 @@ __device__ __forceinline__ void commit_vertex(void *dst, const void *src, int by
   }
 }
 
-__device__ void scatter_tile(const ScatterArgs &a, int t, int n, int T, ScatterSmem &sm) {
+// vertexData[frontier vertex i] = vertexNew[i] for the nf active vertices
+// (grid-stride over the whole launch).
+__device__ __forceinline__ void commit_frontier(const ScatterArgs &a, int nf) {
+  const int stride = gridDim.x * blockDim.x;
+  char *vd = reinterpret_cast<char *>(a.vertexData);
+  const char *vn = reinterpret_cast<const char *>(a.vertexNew);
+  const int vb = a.vertexBytes;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += stride) {
+    const int v = a.rangeMode ? a.rangeStart + i : a.frontVid[i];
+    commit_vertex(vd + (size_t)v * vb, vn + (size_t)i * vb, vb);
+  }
+}
+
+__device__ inline void scatter_tile(const ScatterArgs &a, int t, int n, int T, ScatterSmem &sm) {
   const int tid = threadIdx.x;
   const long long total = (long long)n + T;
   const int d0 = t * GAS_SCATTER_TILE;
@@ -152,7 +165,7 @@ __device__ void scatter_tile(const ScatterArgs &a, int t, int n, int T, ScatterS
                                             a.errWord, sm.app);
 }
 
-__global__ void __launch_bounds__(kSNT) scatter_activate_kernel(const ScatterArgs a) {
+static __global__ void __launch_bounds__(kSNT) scatter_activate_kernel(const ScatterArgs a) {
   __shared__ ScatterSmem sm;
   const unsigned long long sc = *a.scatCount;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -168,14 +181,7 @@ __global__ void __launch_bounds__(kSNT) scatter_activate_kernel(const ScatterArg
       nf = (int)(*a.frontCount >> 32);
       if (nf > a.capacity) nf = a.capacity;
     }
-    const int stride = gridDim.x * blockDim.x;
-    char *vd = reinterpret_cast<char *>(a.vertexData);
-    const char *vn = reinterpret_cast<const char *>(a.vertexNew);
-    const int vb = a.vertexBytes;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += stride) {
-      const int v = a.rangeMode ? a.rangeStart + i : a.frontVid[i];
-      commit_vertex(vd + (size_t)v * vb, vn + (size_t)i * vb, vb);
-    }
+    commit_frontier(a, nf);
   }
   int n = (int)(sc >> 32);
   if (n > a.capacity) n = a.capacity;
@@ -195,7 +201,7 @@ __global__ void __launch_bounds__(kSNT) scatter_activate_kernel(const ScatterArg
 
 // Merge-path splits of a vertex range [rangeStart, rangeStart+n) against
 // its in-edges, for gather tiles of GAS_GATHER_TILE items.
-__global__ void range_split_kernel(const int32_t *inOffsets, int rangeStart, int n, int T,
+static __global__ void range_split_kernel(const int32_t *inOffsets, int rangeStart, int n, int T,
                                    int32_t *split, int nsplit) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nsplit) return;

@@ -32,7 +32,7 @@
 #include <type_traits>
 
 #include "../gas_gb300_core.h"
-#include "detail/gather.cuh"
+#include "detail/persistent.cuh"
 
 namespace gas {
 
@@ -121,10 +121,14 @@ class EngineGPU {
   // returns the number of rounds executed.
   int32_t runFor(int32_t maxIters) {
     int32_t it = 0;
-    note(gas_core_run(core_, maxIters, ProgramHaveGather<Program>::value ? 1 : 0, &launch, this,
-                      &it));
+    note(gas_core_run_persistent(core_, maxIters, ProgramHaveGather<Program>::value ? 1 : 0,
+                                 persistent_ ? &launchRun : nullptr, &launch, this, &it));
     return it;
   }
+
+  // run() as one persistent cooperative kernel (default) or one launch per
+  // phase and round.
+  void setPersistent(bool on) { persistent_ = on; }
 
   // Round number handed to apply(v, g, round) by the stepwise API.
   void setIteration(int32_t it) { note(gas_core_set_iteration(core_, it)); }
@@ -157,8 +161,33 @@ class EngineGPU {
     return cudaGetLastError() == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
   }
 
+  static gas_status launchRun(void *user, const gas_run_args *ra, void *stream) {
+    EngineGPU *self = static_cast<EngineGPU *>(user);
+    if (self->runGrid_ == 0) {
+      int dev = 0, sms = 0, per = 0, coop = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per, detail::run_persistent_kernel<Program>, detail::kGNT, 0);
+      self->runGrid_ = (coop && per > 0 && sms > 0) ? per * sms : -1;
+    }
+    if (self->runGrid_ < 0) return GAS_ERR_UNSUPPORTED;
+    void *args[] = {const_cast<gas_run_args *>(ra)};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)detail::run_persistent_kernel<Program>,
+                                                dim3(self->runGrid_), dim3(detail::kGNT), args,
+                                                0, (cudaStream_t)stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge) {
+      cudaGetLastError();
+      return GAS_ERR_UNSUPPORTED;
+    }
+    return e == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
+  }
+
   gas_core *core_ = nullptr;
   gas_status status_ = GAS_OK;
+  bool persistent_ = true;
+  int runGrid_ = 0;
   VertexData *vdHost_ = nullptr;
   EdgeData *edHost_ = nullptr;
   int grid_ = 0;

@@ -81,11 +81,44 @@ typedef struct {
   int32_t haveGather;
 } gas_gather_args;
 
+/* Arguments of one persistent run() launch: every round of gather/apply,
+ * commit + scatter/activate and frontier swap in a single cooperative
+ * kernel, the phases separated by bounded grid barriers. */
+typedef struct {
+  gas_gather_args g;          /* graph, vertex data, carry arrays, ...      */
+  const int32_t *outDests;    /* CSR destinations [nEdges]                  */
+  int32_t vertexBytes;
+  int32_t maxGatherTiles;
+  int32_t *frontVid[2];
+  int32_t *frontPre[2];
+  int32_t *frontSplit[2];
+  int32_t *rangeSplit;
+  int32_t *scatVidB[2];
+  int32_t *scatPreB[2];
+  int32_t *scatSplitB[2];
+  unsigned long long *frontCnt[2];
+  unsigned long long *scatCnt[2];
+  int32_t *mark;
+  unsigned long long *stats;  /* 2 words per round, maxStatRounds rounds    */
+  int32_t maxStatRounds;
+  int32_t cur;                /* frontier buffer of round 0 (list mode)     */
+  int32_t sidx;               /* scatter list of round 0                    */
+  int32_t maxRounds;          /* 0 = until no vertex is active              */
+  unsigned epochBase;         /* carry-flag epoch of round 0                */
+  int32_t stampBase;          /* activation stamp of round 0                */
+  unsigned *barrier;          /* [2]: arrival count, generation             */
+  int32_t *roundsOut;         /* rounds executed                            */
+} gas_run_args;
+
 typedef struct gas_core_s gas_core;
 
 /* Launches the caller's gather+apply kernel for `args` on `stream`. */
 typedef gas_status (*gas_gather_launch_fn)(void *user, const gas_gather_args *args,
                                            void *stream);
+/* Launches the caller's persistent run kernel (cooperative launch).
+ * Returns GAS_ERR_UNSUPPORTED when it cannot be launched co-resident; the
+ * core then falls back to one launch per phase. */
+typedef gas_status (*gas_run_launch_fn)(void *user, const gas_run_args *args, void *stream);
 
 GAS_API gas_status gas_core_create(int32_t device, void *stream, gas_core **out);
 GAS_API gas_status gas_core_destroy(gas_core *c);
@@ -124,6 +157,14 @@ GAS_API gas_status gas_core_next_iter(gas_core *c);
 GAS_API gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
                                 gas_gather_launch_fn launch, void *user,
                                 int32_t *iterations);
+
+/* run() as one persistent cooperative launch (runLaunch); falls back to
+ * gas_core_run's per-phase launches when runLaunch is NULL or reports
+ * GAS_ERR_UNSUPPORTED. */
+GAS_API gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGather,
+                                           gas_run_launch_fn runLaunch,
+                                           gas_gather_launch_fn launch, void *user,
+                                           int32_t *iterations);
 
 GAS_API gas_status gas_core_round_stats(gas_core *c, int32_t capacity, int64_t *active,
                                         int64_t *gathered, int64_t *ret,

@@ -91,6 +91,7 @@ SIGNATURES = {
     "gas_core_scatter_activate": (_I32, [_P]),
     "gas_core_next_iter": (_I32, [_P]),
     "gas_core_run": (_I32, [_P, _I32, _I32, _P, _P, _PI32]),
+    "gas_core_run_persistent": (_I32, [_P, _I32, _I32, _P, _P, _P, _PI32]),
     "gas_core_round_stats": (_I32, [_P, _I32, _PI64, _PI64, _PI64, _PI64, _PI32]),
     "gas_core_last_run_ms": (_I32, [_P, C.POINTER(C.c_float)]),
     "gas_core_sync": (_I32, [_P]),

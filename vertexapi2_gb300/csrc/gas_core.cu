@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -82,8 +83,9 @@ struct Ctl {
   unsigned long long fcnt[2];
   unsigned long long scnt[2];
   unsigned tile[2];
-  unsigned err;
-  unsigned pad;
+  unsigned bar[2];  // persistent-kernel grid barrier: arrivals, generation
+  int32_t rounds;   // rounds executed by the last persistent run
+  unsigned err;     // device error bits (kept across set_active)
 };
 
 enum DirtyBit : unsigned {
@@ -437,7 +439,7 @@ gas_status gas_core_set_active(gas_core *c, int32_t start, int32_t end) {
     return fail(GAS_ERR_INVALID, "active range [%d, %d) outside [0, %d]", start, end, c->nV);
   gas_status st = set_device(c);
   if (st) return st;
-  cudaError_t e = cudaMemsetAsync(c->ctl, 0, sizeof(Ctl) - 8, c->stream);  // keep err
+  cudaError_t e = cudaMemsetAsync(c->ctl, 0, offsetof(Ctl, err), c->stream);  // keep err
   if (e != cudaSuccess) return cuda_fail(e, "set_active reset");
   c->dirty = 0;
   c->rangeMode = true;
@@ -624,6 +626,7 @@ gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
   if (st) return st;
   cudaEventRecord(c->t0, c->stream);
   const int32_t base = c->iteration;
+  const int32_t round0 = c->round;
   int32_t done = -1, launched = 0;
   if (n0 == 0) done = 0;
   for (int32_t r = 0; done < 0 && (maxIters <= 0 || r < maxIters); ++r) {
@@ -669,6 +672,7 @@ gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
       }
   }
   c->iteration = base + done;
+  c->round = round0 + done;  // trailing launches saw an empty frontier
   cudaEventElapsedTime(&c->lastMs, c->t0, c->t1);
   c->gatherMs = c->scatterMs = 0.f;
   c->gatherLaunches = c->scatterLaunches = 0;
@@ -683,6 +687,113 @@ gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
     c->gatherLaunches = c->scatterLaunches = launched;
   }
   if (iterations) *iterations = done;
+  return check_device_error(c);
+}
+
+gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGather,
+                                   gas_run_launch_fn runLaunch, gas_gather_launch_fn launch,
+                                   void *user, int32_t *iterations) {
+  if (!c) return fail(GAS_ERR_INVALID, "run: engine is NULL");
+  if (!runLaunch || c->profiling) return gas_core_run(c, maxIters, haveGather, launch, user, iterations);
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  gas_status st = set_device(c);
+  if (st) return st;
+  if (iterations) *iterations = 0;
+  int32_t n0 = 0;
+  st = gas_core_count_active(c, &n0);
+  if (st) return st;
+  if (n0 == 0) return GAS_OK;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  if (c->epoch > 0xC0000000u) {
+    A(cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream));
+    c->epoch = 0;
+  }
+  if (c->stamp > 0x40000000) {
+    A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
+    c->stamp = 0;
+  }
+  A(cudaMemsetAsync(&c->ctl->scnt[0], 0, sizeof(c->ctl->scnt), c->stream));
+  A(cudaMemsetAsync(&c->ctl->fcnt[c->cur ^ 1], 0, 8, c->stream));
+  A(cudaMemsetAsync(&c->ctl->bar[0], 0, sizeof(c->ctl->bar) + sizeof(int32_t), c->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "run setup");
+
+  gas_run_args ra;
+  memset(&ra, 0, sizeof(ra));
+  gas_gather_args &a = ra.g;
+  a.nVertices = c->nV;
+  a.nEdges = c->nE;
+  a.inOffsets = c->inOff;
+  a.inSources = c->inSrc;
+  a.outOffsets = c->outOff;
+  a.edgeData = c->ed;
+  a.vertexData = c->vd;
+  a.vertexNew = c->vnew;
+  a.rangeMode = c->rangeMode ? 1 : 0;
+  a.rangeStart = c->rstart;
+  a.rangeCount = c->rcount;
+  a.rangeBase = c->rangeMode ? c->hInOff[c->rstart] : 0;
+  a.capacity = c->nV;
+  a.maxScatTiles = c->maxScatTiles;
+  a.carryVal = c->carryVal;
+  a.carryFlag = c->carryFlag;
+  a.errWord = &c->ctl->err;
+  a.iteration = c->iteration;
+  a.haveGather = haveGather ? 1 : 0;
+  ra.outDests = c->outDst;
+  ra.vertexBytes = c->vertexBytes;
+  ra.maxGatherTiles = c->maxGatherTiles;
+  for (int k = 0; k < 2; ++k) {
+    ra.frontVid[k] = c->fvid[k];
+    ra.frontPre[k] = c->fpre[k];
+    ra.frontSplit[k] = c->fsplit[k];
+    ra.scatVidB[k] = c->svid[k];
+    ra.scatPreB[k] = c->spre[k];
+    ra.scatSplitB[k] = c->ssplit[k];
+    ra.frontCnt[k] = &c->ctl->fcnt[k];
+    ra.scatCnt[k] = &c->ctl->scnt[k];
+  }
+  ra.rangeSplit = c->rsplit;
+  ra.mark = c->mark;
+  ra.stats = c->stats + 2 * (size_t)std::min(c->round, kMaxRounds);
+  ra.maxStatRounds = std::max(0, kMaxRounds - c->round);
+  ra.cur = c->cur;
+  ra.sidx = c->sidx;
+  ra.maxRounds = maxIters > 0 ? maxIters : 0;
+  ra.epochBase = c->epoch + 1;
+  ra.stampBase = c->stamp + 1;
+  ra.barrier = &c->ctl->bar[0];
+  ra.roundsOut = &c->ctl->rounds;
+
+  cudaEventRecord(c->t0, c->stream);
+  st = runLaunch(user, &ra, (void *)c->stream);
+  if (st == GAS_ERR_UNSUPPORTED) return gas_core_run(c, maxIters, haveGather, launch, user, iterations);
+  if (st) return st;
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "persistent run launch");
+  cudaEventRecord(c->t1, c->stream);
+  int32_t rounds = 0;
+  A(cudaMemcpyAsync(&rounds, &c->ctl->rounds, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  A(cudaStreamSynchronize(c->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "persistent run");
+  cudaEventElapsedTime(&c->lastMs, c->t0, c->t1);
+  const int32_t R = rounds;
+  if (R & 1) {
+    c->cur ^= 1;
+    c->sidx ^= 1;
+  }
+  if (R > 0) c->rangeMode = false;
+  c->epoch += (unsigned)R;
+  c->stamp += R;
+  c->iteration += R;
+  c->round += R;
+  c->dirty |= kF0 | kF1 | kS0 | kS1;
+  c->pendingCommit = false;
+  c->haveScatList = false;
+  c->countValid = false;
+  if (iterations) *iterations = R;
   return check_device_error(c);
 }
 
