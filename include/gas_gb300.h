@@ -144,6 +144,13 @@ GAS_API gas_status gas_engine_set_profiling(gas_engine *e, int32_t enabled);
 GAS_API gas_status gas_engine_kernel_times(gas_engine *e, float *gatherMs, float *scatterMs,
                                            int32_t *gatherLaunches, int32_t *scatterLaunches);
 
+/* Launch shape of run(): persistent != 0 runs every round in one
+ * cooperative kernel (the default), 0 launches each phase of each round;
+ * runBlocksPerSM bounds the persistent kernel's CTAs per SM (0 = as many as
+ * fit).  Results do not depend on either. */
+GAS_API gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
+                                                int32_t runBlocksPerSM);
+
 /* ---------------- status / diagnostics ---------------------------------- */
 GAS_API const char *gas_status_string(gas_status s);
 GAS_API const char *gas_last_error(void);

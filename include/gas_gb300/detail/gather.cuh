@@ -19,6 +19,12 @@
 //     refgas.h:143-167);
 //   * vertices whose apply returned true are appended to the scatter list
 //     with their out-degree prefix and the scatter kernel's tile splits.
+//
+// Rounds whose frontier has no vertex of in-degree above
+// GAS_TPV_MAX_DEGREE (lattices, road networks) run one thread per vertex
+// instead: no merge path, block scan or look-back, and the edges of a
+// vertex are folded left to right in CSC order, exactly as
+// refgas.h:147-158 folds them.
 #pragma once
 
 #include <type_traits>
@@ -72,13 +78,20 @@ __device__ __forceinline__ const typename P::EdgeData *edge_ptr(const void *ed, 
   return reinterpret_cast<const typename P::EdgeData *>(ed) + e;
 }
 
+// The merge-path arrays are dead once block_append stages its output (its
+// first internal barrier follows the last read of vid), so they share
+// storage with the staging area.
 template <class P>
 struct GatherSmem {
-  int32_t end[kGTILE];       // tile-local edge index at which vertex i0+m ends
-  int32_t vid[kGTILE + 1];   // vertex id of frontier entry i0+m
-  int32_t base[kGTILE + 1];  // CSC position = frontier edge index + base
+  union {
+    struct {
+      int32_t end[kGTILE];       // tile-local edge index at which vertex i0+m ends
+      int32_t vid[kGTILE + 1];   // vertex id of frontier entry i0+m
+      int32_t base[kGTILE + 1];  // CSC position = frontier edge index + base
+    };
+    AppendSmem<kGNT, kGVT> app;
+  };
   SegScanSmem<typename P::GatherResult, kGNT> seg;
-  AppendSmem<kGNT, kGVT> app;
   int32_t headPre;
   unsigned lookHas;
   typename P::GatherResult lookVal;
@@ -91,11 +104,49 @@ __device__ __forceinline__ void frontier_size(const gas_gather_args &a, int &n, 
     n = a.rangeCount;
     T = a.inOffsets[a.rangeStart + a.rangeCount] - a.rangeBase;
   } else {
-    unsigned long long c = *a.frontCount;
+    unsigned long long c = *a.front.count;
     n = (int)(c >> 32);
     T = (int)(c & 0xffffffffull);
     if (n > a.capacity) n = a.capacity;  // only after a reported overflow
   }
+}
+
+__device__ __forceinline__ unsigned frontier_max_degree(const gas_gather_args &a) {
+  return a.rangeMode ? (unsigned)a.rangeMaxDeg : *a.front.maxDeg;
+}
+
+// Entry i of the current frontier: vertex, in-edge prefix and end, CSC begin.
+__device__ __forceinline__ void front_entry(const gas_gather_args &a, int i, int n, int T,
+                                            int &v, int &pre, int &end, int &beg) {
+  if (a.rangeMode) {
+    v = a.rangeStart + i;
+    beg = a.inOffsets[v];
+    pre = beg - a.rangeBase;
+    end = a.inOffsets[v + 1] - a.rangeBase;
+  } else {
+    v = a.front.vid[i];
+    pre = a.front.pre[i];
+    end = (i + 1 < n) ? a.front.pre[i + 1] : T;
+    beg = a.front.beg[i];
+  }
+}
+
+// Gather tiles of the current round: mode and count.
+__device__ __forceinline__ int gather_tiles(const gas_gather_args &a, int n, int T, bool &tpv) {
+  tpv = a.haveGather && frontier_max_degree(a) <= GAS_TPV_MAX_DEGREE;
+  long long items;
+  int tile;
+  if (!a.haveGather) {
+    items = n;
+    tile = kGTILE;
+  } else if (tpv) {
+    items = n;
+    tile = GAS_TPV_TILE;
+  } else {
+    items = (long long)n + T;
+    tile = kGTILE;
+  }
+  return (int)((items + tile - 1) / tile);
 }
 
 template <class P>
@@ -106,8 +157,9 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
   const long long total = (long long)n + T;
   const int d0 = t * kGTILE;
   const int d1 = (int)min((long long)d0 + kGTILE, total);
-  const int i0 = a.frontSplit[t];
-  const int i1 = (d1 == total) ? n : a.frontSplit[t + 1];
+  const int32_t *split = a.rangeMode ? a.rangeSplit : a.front.split;
+  const int i0 = split[t];
+  const int i1 = (d1 == total) ? n : split[t + 1];
   const int j0 = d0 - i0, j1 = d1 - i1;
   const int nb = i1 - i0;  // vertices ending in this tile
   const int na = j1 - j0;  // edges in this tile
@@ -115,19 +167,10 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
   const VD *vd = reinterpret_cast<const VD *>(a.vertexData);
 
   for (int m = tid; m < nload; m += kGNT) {
-    const int i = i0 + m;
-    int v, pre, end;
-    if (a.rangeMode) {
-      v = a.rangeStart + i;
-      pre = a.inOffsets[v] - a.rangeBase;
-      end = a.inOffsets[v + 1] - a.rangeBase;
-    } else {
-      v = a.frontVid[i];
-      pre = a.frontPre[i];
-      end = (i + 1 < n) ? a.frontPre[i + 1] : T;
-    }
+    int v, pre, end, beg;
+    front_entry(a, i0 + m, n, T, v, pre, end, beg);
     sm.vid[m] = v;
-    sm.base[m] = a.inOffsets[v] - pre;
+    sm.base[m] = beg - pre;
     if (m < nb) sm.end[m] = end - j0;
     if (m == 0) sm.headPre = pre;
   }
@@ -169,17 +212,27 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
     }
   }
 
-  // ---- loads first (independent), then gatherMap values
-  int src[kGVT];
+  // ---- independent loads first: in-edge sources, and for vertex ends the
+  // vertex data and CSR range that apply / the scatter list need
+  int src[kGVT], obeg[kGVT], oend[kGVT];
 #pragma unroll
-  for (int v = 0; v < kGVT; ++v) src[v] = (kind[v] == 1) ? __ldg(a.inSources + phys[v]) : 0;
+  for (int v = 0; v < kGVT; ++v) {
+    src[v] = 0;
+    obeg[v] = oend[v] = 0;
+    if (kind[v] == 1) src[v] = __ldg(a.inSources + phys[v]);
+    if (kind[v] == 2) {
+      const int vx = sm.vid[vloc[v]];
+      obeg[v] = a.outOffsets[vx];
+      oend[v] = a.outOffsets[vx + 1];
+    }
+  }
   GR val[kGVT];
 #pragma unroll
   for (int v = 0; v < kGVT; ++v)
     if (kind[v] == 1)
       val[v] = P::gatherMap(vd + sm.vid[vloc[v]], vd + src[v], edge_ptr<P>(a.edgeData, phys[v]));
 
-  // ---- thread-sequential fold; seg_*[v] holds the segment ending at item v
+  // ---- thread-sequential fold; seg*[v] holds the segment ending at item v
   unsigned has = 0u;
   GR acc;
   bool segHas[kGVT];
@@ -300,12 +353,52 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
       if (r) {
         ok[v] = true;
         ovid[v] = vx;
-        odeg[v] = a.outOffsets[vx + 1] - a.outOffsets[vx];
+        odeg[v] = oend[v] - obeg[v];
       }
     }
   }
-  block_append<kGNT, kGVT, kSTILE>(ok, ovid, odeg, a.scatVid, a.scatPre, a.scatSplit,
-                                   a.maxScatTiles, a.scatCount, a.capacity, a.errWord, sm.app);
+  block_append<kGNT, kGVT, kSTILE>(ok, ovid, odeg, obeg, a.scat, a.maxScatTiles, a.capacity,
+                                   a.errWord, sm.app);
+}
+
+// Low-degree rounds: one thread per active vertex, its (<= GAS_TPV_MAX_DEGREE)
+// in-edges folded left to right from gatherZero, as refgas.h:147-158.
+template <class P>
+__device__ void tpv_gather_tile(const gas_gather_args &a, int t, int n, int T,
+                                GatherSmem<P> &sm) {
+  typedef typename P::VertexData VD;
+  typedef typename P::GatherResult GR;
+  constexpr int D = GAS_TPV_MAX_DEGREE;
+  const VD *vd = reinterpret_cast<const VD *>(a.vertexData);
+  VD *vnew = reinterpret_cast<VD *>(a.vertexNew);
+  const int i = t * GAS_TPV_TILE + threadIdx.x;
+  bool ok[1] = {false};
+  int32_t ov[1] = {0}, od[1] = {0}, ob[1] = {0};
+  if (i < n) {
+    int v, pre, end, beg;
+    front_entry(a, i, n, T, v, pre, end, beg);
+    const int deg = end - pre;
+    const int obeg = a.outOffsets[v], oend = a.outOffsets[v + 1];
+    int src[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) src[k] = k < deg ? __ldg(a.inSources + beg + k) : 0;
+    GR acc = P::gatherZero;
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      if (k < deg)
+        acc = P::gatherReduce(acc, P::gatherMap(vd + v, vd + src[k], edge_ptr<P>(a.edgeData, beg + k)));
+    VD tmp = vd[v];
+    const bool r = do_apply<P>(&tmp, acc, a.iteration);
+    vnew[i] = tmp;
+    if (r) {
+      ok[0] = true;
+      ov[0] = v;
+      od[0] = oend - obeg;
+      ob[0] = obeg;
+    }
+  }
+  block_append<kGNT, 1, kSTILE>(ok, ov, od, ob, a.scat, a.maxScatTiles, a.capacity, a.errWord,
+                                sm.app);
 }
 
 // apply only (gatherApply(false), gpugas.h:503-512): one thread per active
@@ -317,53 +410,65 @@ __device__ void apply_tile(const gas_gather_args &a, int t, int n, GatherSmem<P>
   VD *vd = reinterpret_cast<VD *>(a.vertexData);
   const GR gz = P::gatherZero;
   bool ok[kGVT];
-  int32_t ovid[kGVT], odeg[kGVT];
+  int32_t ovid[kGVT], odeg[kGVT], obeg[kGVT];
 #pragma unroll
   for (int v = 0; v < kGVT; ++v) {
     ok[v] = false;
     ovid[v] = 0;
     odeg[v] = 0;
+    obeg[v] = 0;
     const int i = t * kGTILE + v * kGNT + threadIdx.x;
     if (i < n) {
-      const int32_t vx = a.rangeMode ? a.rangeStart + i : a.frontVid[i];
+      const int32_t vx = a.rangeMode ? a.rangeStart + i : a.front.vid[i];
+      const int ob = a.outOffsets[vx], oe = a.outOffsets[vx + 1];
       VD tmp = vd[vx];
       const bool r = do_apply<P>(&tmp, gz, a.iteration);
       vd[vx] = tmp;
       if (r) {
         ok[v] = true;
         ovid[v] = vx;
-        odeg[v] = a.outOffsets[vx + 1] - a.outOffsets[vx];
+        odeg[v] = oe - ob;
+        obeg[v] = ob;
       }
     }
   }
-  block_append<kGNT, kGVT, kSTILE>(ok, ovid, odeg, a.scatVid, a.scatPre, a.scatSplit,
-                                   a.maxScatTiles, a.scatCount, a.capacity, a.errWord, sm.app);
+  block_append<kGNT, kGVT, kSTILE>(ok, ovid, odeg, obeg, a.scat, a.maxScatTiles, a.capacity,
+                                   a.errWord, sm.app);
 }
 
-// Persistent-style grid: blocks take tiles in order from a counter, so a
+template <class P>
+__device__ __forceinline__ void gather_dispatch(const gas_gather_args &a, int t, int n, int T,
+                                                bool tpv, GatherSmem<P> &sm) {
+  if (!a.haveGather)
+    apply_tile<P>(a, t, n, sm);
+  else if (tpv)
+    tpv_gather_tile<P>(a, t, n, T, sm);
+  else
+    gather_tile<P>(a, t, n, T, sm);
+}
+
+// One launch per phase: blocks take tiles in order from a counter, so a
 // tile whose look-back waits on earlier tiles only waits on running CTAs.
 template <class P>
 __global__ void __launch_bounds__(kGNT) gather_apply_kernel(const gas_gather_args a) {
   __shared__ GatherSmem<P> sm;
   int n, T;
   frontier_size(a, n, T);
+  bool tpv;
+  const int ntiles = gather_tiles(a, n, T, tpv);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *a.resetCount = 0ull;
+    *a.resetMaxDeg = 0u;
     *a.resetTile = 0u;
     if (a.statSlot) a.statSlot[0] = ((unsigned long long)n << 32) | (unsigned)T;
   }
-  const long long items = a.haveGather ? (long long)n + T : (long long)n;
-  const int ntiles = (int)((items + kGTILE - 1) / kGTILE);
   for (;;) {
     if (threadIdx.x == 0) sm.tile = (int)atomicAdd(a.tileCounter, 1u);
     __syncthreads();
     const int t = sm.tile;
     __syncthreads();
     if (t >= ntiles) break;
-    if (a.haveGather)
-      gather_tile<P>(a, t, n, T, sm);
-    else
-      apply_tile<P>(a, t, n, sm);
+    gather_dispatch<P>(a, t, n, T, tpv, sm);
     __syncthreads();
   }
 }

@@ -85,7 +85,9 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
   sa.tileCounter = nullptr;
   sa.resetTile = nullptr;
   sa.resetScatCount = nullptr;
+  sa.resetScatMaxDeg = nullptr;
   sa.errWord = a.errWord;
+  sa.statSlot = nullptr;
 
   int cur = ra.cur, sidx = ra.sidx;
   bool rangeMode = a.rangeMode != 0;
@@ -94,48 +96,35 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
     if (ra.maxRounds > 0 && r >= ra.maxRounds) break;
     // ---- this round's frontier (final since the previous barrier)
     a.rangeMode = rangeMode ? 1 : 0;
-    a.frontVid = ra.frontVid[cur];
-    a.frontPre = ra.frontPre[cur];
-    a.frontCount = ra.frontCnt[cur];
-    a.frontSplit = rangeMode ? ra.rangeSplit : ra.frontSplit[cur];
-    a.scatVid = ra.scatVidB[sidx];
-    a.scatPre = ra.scatPreB[sidx];
-    a.scatSplit = ra.scatSplitB[sidx];
-    a.scatCount = ra.scatCnt[sidx];
+    a.front = ra.frontL[cur];
+    a.scat = ra.scatL[sidx];
     a.epoch = ra.epochBase + (unsigned)r;
     a.iteration = ra.g.iteration + r;
     int n, T;
     frontier_size(a, n, T);
     if (n == 0) break;  // uniform: every block read the same count
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-      *ra.frontCnt[cur ^ 1] = 0ull;    // appended by this round's scatter
-      *ra.scatCnt[sidx ^ 1] = 0ull;    // appended by the next round's gather
+      *ra.frontL[cur ^ 1].count = 0ull;  // appended by this round's scatter
+      *ra.frontL[cur ^ 1].maxDeg = 0u;
+      *ra.scatL[sidx ^ 1].count = 0ull;  // appended by the next round's gather
+      *ra.scatL[sidx ^ 1].maxDeg = 0u;
     }
     // ---- gather/apply
-    const long long itemsG = a.haveGather ? (long long)n + T : (long long)n;
-    const int ntG = (int)((itemsG + kGTILE - 1) / kGTILE);
+    bool tpvG;
+    const int ntG = gather_tiles(a, n, T, tpvG);
     for (int t = blockIdx.x; t < ntG; t += gridDim.x) {
-      if (a.haveGather)
-        gather_tile<P>(a, t, n, T, sm.g);
-      else
-        apply_tile<P>(a, t, n, sm.g);
+      gather_dispatch<P>(a, t, n, T, tpvG, sm.g);
       __syncthreads();
     }
     if (!grid_barrier(ra.barrier, a.errWord)) break;
     // ---- commit + scatter/activate
-    sa.scatVid = a.scatVid;
-    sa.scatPre = a.scatPre;
-    sa.scatSplit = a.scatSplit;
-    sa.scatCount = a.scatCount;
+    sa.scat = a.scat;
     sa.rangeMode = a.rangeMode;
-    sa.frontVid = a.frontVid;
-    sa.frontCount = a.frontCount;
-    sa.nextVid = ra.frontVid[cur ^ 1];
-    sa.nextPre = ra.frontPre[cur ^ 1];
-    sa.nextSplit = ra.frontSplit[cur ^ 1];
-    sa.nextCount = ra.frontCnt[cur ^ 1];
+    sa.frontVid = a.front.vid;
+    sa.frontCount = a.front.count;
+    sa.next = ra.frontL[cur ^ 1];
     sa.stamp = ra.stampBase + r;
-    const unsigned long long sc = *a.scatCount;
+    const unsigned long long sc = *a.scat.count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && r < ra.maxStatRounds) {
       ra.stats[2 * (size_t)r] = ((unsigned long long)n << 32) | (unsigned)T;
       ra.stats[2 * (size_t)r + 1] = sc;
@@ -144,9 +133,13 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
     int ns = (int)(sc >> 32);
     if (ns > a.capacity) ns = a.capacity;
     const int Ts = (int)(sc & 0xffffffffull);
-    const int ntS = (int)(((long long)ns + Ts + GAS_SCATTER_TILE - 1) / GAS_SCATTER_TILE);
+    bool tpvS;
+    const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
     for (int t = blockIdx.x; t < ntS; t += gridDim.x) {
-      scatter_tile(sa, t, ns, Ts, sm.s);
+      if (tpvS)
+        tpv_scatter_tile(sa, t, ns, Ts, sm.s);
+      else
+        scatter_tile(sa, t, ns, Ts, sm.s);
       __syncthreads();
     }
     if (!grid_barrier(ra.barrier, a.errWord)) break;

@@ -227,40 +227,48 @@ __device__ __forceinline__ void block_seg_scan(const SegVal<T> &x, SegVal<T> &ex
 }
 
 // ---------------------------------------------------------------------------
-// block_append: every thread offers up to K (vertex, degree) entries in
-// static slots ok[k]/vid[k]/deg[k].  The block reserves (count, degree sum)
-// with one atomicAdd on the packed counter (count << 32 | degree sum), so
-// positions and exclusive degree prefixes of all batches agree.  It then
-// writes, for every consumer tile boundary b = t*TILE falling inside this
-// batch's merged (entries + degrees) range, the number of entries whose
-// end precedes b -- the merge-path split of tile t.
+// block_append: every thread offers up to K vertices in static slots
+// ok[k] / vid[k] / deg[k] / beg[k] (deg = the degree the list's consumer
+// walks, beg = that vertex's CSC/CSR begin offset).  The block reserves
+// (count, degree sum) with one atomicAdd on the list's packed counter
+// (count << 32 | degree sum), so positions and exclusive degree prefixes
+// of all batches agree, raises the list's maximum degree with one
+// atomicMax, and writes, for every consumer tile boundary b = t*TILE
+// inside this batch's merged (entries + degrees) range, the number of
+// entries whose end precedes b -- the merge-path split of tile t.
 template <int NT, int K>
 struct AppendSmem {
   int32_t vid[NT * K + 1];
   int32_t pre[NT * K + 1];
+  int32_t beg[NT * K + 1];
   ScanU64Smem<NT> scan;
   unsigned long long base;
+  unsigned maxd;
 };
 
-template <int NT, int K, int TILE>
+template <int NT, int K, int TILE, int KS>
 __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t (&vid)[K],
-                                             const int32_t (&deg)[K], int32_t *outVid,
-                                             int32_t *outPre, int32_t *outSplit,
-                                             int32_t maxSplit,
-                                             unsigned long long *outCount, int32_t capacity,
-                                             unsigned *errWord, AppendSmem<NT, K> &sm) {
-  unsigned cnt = 0, esum = 0;
+                                             const int32_t (&deg)[K], const int32_t (&beg)[K],
+                                             const gas_vertex_list &out, int32_t maxSplit,
+                                             int32_t capacity, unsigned *errWord,
+                                             AppendSmem<NT, KS> &sm) {
+  static_assert(K <= KS, "staging area too small");
+  unsigned cnt = 0, esum = 0, dmax = 0;
 #pragma unroll
   for (int k = 0; k < K; ++k)
     if (ok[k]) {
       ++cnt;
       esum += (unsigned)deg[k];
+      dmax = max(dmax, (unsigned)deg[k]);
     }
+  if (threadIdx.x == 0) sm.maxd = 0u;
   unsigned long long mine = ((unsigned long long)cnt << 32) | esum;
   unsigned long long excl, total;
   block_exclusive_scan_u64<NT>(mine, excl, total, sm.scan);
   if (total == 0ull) return;  // block-uniform
-  if (threadIdx.x == 0) sm.base = atomicAdd(outCount, total);
+  const unsigned wmax = __reduce_max_sync(kFullMask, dmax);
+  if ((threadIdx.x & 31) == 0 && wmax) atomicMax(&sm.maxd, wmax);
+  if (threadIdx.x == 0) sm.base = atomicAdd(out.count, total);
   int off = (int)(excl >> 32);
   int eoff = (int)(excl & 0xffffffffull);
 #pragma unroll
@@ -268,6 +276,7 @@ __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t 
     if (ok[k]) {
       sm.vid[off] = vid[k];
       sm.pre[off] = eoff;
+      sm.beg[off] = beg[k];
       ++off;
       eoff += deg[k];
     }
@@ -275,6 +284,7 @@ __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t 
   const int Esum = (int)(total & 0xffffffffull);
   if (threadIdx.x == 0) sm.pre[R] = Esum;
   __syncthreads();
+  if (threadIdx.x == 0 && sm.maxd) atomicMax(out.maxDeg, sm.maxd);
   const unsigned long long base = sm.base;
   const long long qpos = (long long)(base >> 32);
   const long long epos = (long long)(base & 0xffffffffull);
@@ -284,8 +294,9 @@ __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t 
     return;
   }
   for (int m = threadIdx.x; m < R; m += NT) {
-    outVid[qpos + m] = sm.vid[m];
-    outPre[qpos + m] = (int32_t)(epos + sm.pre[m]);
+    out.vid[qpos + m] = sm.vid[m];
+    out.pre[qpos + m] = (int32_t)(epos + sm.pre[m]);
+    out.beg[qpos + m] = sm.beg[m];
   }
   // split hints for boundaries b in [D, D + R + Esum)
   const long long D = qpos + epos;
@@ -303,7 +314,7 @@ __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t 
       else
         hi = mid;
     }
-    if (tb < maxSplit) outSplit[tb] = (int32_t)(qpos + lo);
+    if (tb < maxSplit) out.split[tb] = (int32_t)(qpos + lo);
   }
   __syncthreads();
 }

@@ -12,7 +12,10 @@
 //   * deduplicates destinations with a per-vertex round stamp
 //     (one atomicExch per first visit, none afterwards) instead of sorting;
 //   * appends newly active vertices to the next frontier with their
-//     in-degree prefix and the next gather's tile splits (block_append).
+//     in-degree prefix, CSC begin and the next gather's tile splits
+//     (block_append);
+//   * lists whose out-degrees are all <= GAS_TPV_MAX_DEGREE are walked one
+//     thread per vertex instead of in merge-path tiles.
 #pragma once
 
 #include "primitives.cuh"
@@ -27,11 +30,7 @@ struct ScatterArgs {
   const int32_t *outOffsets;
   const int32_t *outDests;
   const int32_t *inOffsets;
-  // scatter list built by the gather kernel
-  const int32_t *scatVid;
-  const int32_t *scatPre;
-  const int32_t *scatSplit;
-  const unsigned long long *scatCount;
+  gas_vertex_list scat;  // built by the gather kernel (out-degree prefix)
   // commit of vertexNew for the current frontier
   int32_t commit;
   int32_t vertexBytes;
@@ -42,11 +41,7 @@ struct ScatterArgs {
   int32_t rangeCount;
   const int32_t *frontVid;
   const unsigned long long *frontCount;
-  // next frontier
-  int32_t *nextVid;
-  int32_t *nextPre;
-  int32_t *nextSplit;
-  unsigned long long *nextCount;
+  gas_vertex_list next;  // next frontier (in-degree prefix)
   int32_t maxGatherTiles;
   int32_t capacity;
   // destination dedup
@@ -56,14 +51,19 @@ struct ScatterArgs {
   unsigned *tileCounter;
   unsigned *resetTile;
   unsigned long long *resetScatCount;
+  unsigned *resetScatMaxDeg;
   unsigned *errWord;
   unsigned long long *statSlot;  // round statistics (may be null)
 };
 
 struct ScatterSmem {
-  int32_t end[GAS_SCATTER_TILE];
-  int32_t base[GAS_SCATTER_TILE + 1];
-  AppendSmem<kSNT, kSVT> app;
+  union {
+    struct {
+      int32_t end[GAS_SCATTER_TILE];
+      int32_t base[GAS_SCATTER_TILE + 1];
+    };
+    AppendSmem<kSNT, kSVT> app;  // staging reuses the merge-path arrays
+  };
   int32_t tile;
 };
 
@@ -92,22 +92,47 @@ __device__ __forceinline__ void commit_frontier(const ScatterArgs &a, int nf) {
   }
 }
 
+// Activation of destination u: the in-degree and CSC begin are loaded
+// before the stamp test so both round trips overlap.
+template <int K>
+__device__ __forceinline__ void activate(const ScatterArgs &a, const bool (&isEdge)[K],
+                                         const int32_t (&dst)[K], bool (&ok)[K],
+                                         int32_t (&deg)[K], int32_t (&beg)[K]) {
+#pragma unroll
+  for (int v = 0; v < K; ++v) {
+    ok[v] = false;
+    deg[v] = 0;
+    beg[v] = 0;
+    if (isEdge[v]) {
+      beg[v] = a.inOffsets[dst[v]];
+      deg[v] = a.inOffsets[dst[v] + 1];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < K; ++v) {
+    if (isEdge[v]) {
+      deg[v] -= beg[v];
+      int32_t *mk = a.mark + dst[v];
+      if (__ldcg(mk) != a.stamp && atomicExch(mk, a.stamp) != a.stamp) ok[v] = true;
+    }
+  }
+}
+
 __device__ inline void scatter_tile(const ScatterArgs &a, int t, int n, int T, ScatterSmem &sm) {
   const int tid = threadIdx.x;
   const long long total = (long long)n + T;
   const int d0 = t * GAS_SCATTER_TILE;
   const int d1 = (int)min((long long)d0 + GAS_SCATTER_TILE, total);
-  const int i0 = a.scatSplit[t];
-  const int i1 = (d1 == total) ? n : a.scatSplit[t + 1];
+  const int i0 = a.scat.split[t];
+  const int i1 = (d1 == total) ? n : a.scat.split[t + 1];
   const int j0 = d0 - i0, j1 = d1 - i1;
   const int nb = i1 - i0, na = j1 - j0;
   const int nload = nb + (i1 < n ? 1 : 0);
   for (int m = tid; m < nload; m += kSNT) {
     const int i = i0 + m;
-    const int v = a.scatVid[i];
-    const int pre = a.scatPre[i];
-    const int end = (i + 1 < n) ? a.scatPre[i + 1] : T;
-    sm.base[m] = a.outOffsets[v] - pre;
+    const int pre = a.scat.pre[i];
+    const int end = (i + 1 < n) ? a.scat.pre[i + 1] : T;
+    sm.base[m] = a.scat.beg[i] - pre;
     if (m < nb) sm.end[m] = end - j0;
   }
   __syncthreads();
@@ -147,30 +172,57 @@ __device__ inline void scatter_tile(const ScatterArgs &a, int t, int n, int T, S
 #pragma unroll
   for (int v = 0; v < kSVT; ++v) dst[v] = isEdge[v] ? __ldg(a.outDests + phys[v]) : 0;
   bool ok[kSVT];
-  int32_t deg[kSVT];
+  int32_t deg[kSVT], beg[kSVT];
+  activate<kSVT>(a, isEdge, dst, ok, deg, beg);
+  block_append<kSNT, kSVT, GAS_GATHER_TILE>(ok, dst, deg, beg, a.next, a.maxGatherTiles,
+                                            a.capacity, a.errWord, sm.app);
+}
+
+// Low-degree rounds: one thread per vertex of the scatter list.
+__device__ inline void tpv_scatter_tile(const ScatterArgs &a, int t, int n, int T,
+                                        ScatterSmem &sm) {
+  constexpr int D = GAS_TPV_MAX_DEGREE;
+  const int i = t * GAS_TPV_TILE + threadIdx.x;
+  bool isEdge[D];
+  int32_t dst[D];
+  if (i < n) {
+    const int pre = a.scat.pre[i];
+    const int end = (i + 1 < n) ? a.scat.pre[i + 1] : T;
+    const int b = a.scat.beg[i];
+    const int d = end - pre;
 #pragma unroll
-  for (int v = 0; v < kSVT; ++v) {
-    ok[v] = false;
-    deg[v] = 0;
-    if (isEdge[v]) {
-      int32_t *mk = a.mark + dst[v];
-      if (__ldcg(mk) != a.stamp && atomicExch(mk, a.stamp) != a.stamp) {
-        ok[v] = true;
-        deg[v] = a.inOffsets[dst[v] + 1] - a.inOffsets[dst[v]];
-      }
+    for (int k = 0; k < D; ++k) {
+      isEdge[k] = k < d;
+      dst[k] = k < d ? __ldg(a.outDests + b + k) : 0;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      isEdge[k] = false;
+      dst[k] = 0;
     }
   }
-  block_append<kSNT, kSVT, GAS_GATHER_TILE>(ok, dst, deg, a.nextVid, a.nextPre, a.nextSplit,
-                                            a.maxGatherTiles, a.nextCount, a.capacity,
-                                            a.errWord, sm.app);
+  bool ok[D];
+  int32_t deg[D], beg[D];
+  activate<D>(a, isEdge, dst, ok, deg, beg);
+  block_append<kSNT, D, GAS_GATHER_TILE>(ok, dst, deg, beg, a.next, a.maxGatherTiles,
+                                         a.capacity, a.errWord, sm.app);
+}
+
+// Scatter tiles of a scatter list: mode and count.
+__device__ __forceinline__ int scatter_tiles(const gas_vertex_list &l, int n, int T, bool &tpv) {
+  tpv = *l.maxDeg <= GAS_TPV_MAX_DEGREE;
+  if (tpv) return (n + GAS_TPV_TILE - 1) / GAS_TPV_TILE;
+  return (int)(((long long)n + T + GAS_SCATTER_TILE - 1) / GAS_SCATTER_TILE);
 }
 
 static __global__ void __launch_bounds__(kSNT) scatter_activate_kernel(const ScatterArgs a) {
   __shared__ ScatterSmem sm;
-  const unsigned long long sc = *a.scatCount;
+  const unsigned long long sc = *a.scat.count;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *a.resetTile = 0u;
     *a.resetScatCount = 0ull;
+    *a.resetScatMaxDeg = 0u;
     if (a.statSlot) a.statSlot[1] = sc;
   }
   if (a.commit) {
@@ -186,15 +238,18 @@ static __global__ void __launch_bounds__(kSNT) scatter_activate_kernel(const Sca
   int n = (int)(sc >> 32);
   if (n > a.capacity) n = a.capacity;
   const int T = (int)(sc & 0xffffffffull);
-  const long long items = (long long)n + T;
-  const int ntiles = (int)((items + GAS_SCATTER_TILE - 1) / GAS_SCATTER_TILE);
+  bool tpv;
+  const int ntiles = scatter_tiles(a.scat, n, T, tpv);
   for (;;) {
     if (threadIdx.x == 0) sm.tile = (int)atomicAdd(a.tileCounter, 1u);
     __syncthreads();
     const int t = sm.tile;
     __syncthreads();
     if (t >= ntiles) break;
-    scatter_tile(a, t, n, T, sm);
+    if (tpv)
+      tpv_scatter_tile(a, t, n, T, sm);
+    else
+      scatter_tile(a, t, n, T, sm);
     __syncthreads();
   }
 }

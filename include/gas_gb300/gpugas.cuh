@@ -130,6 +130,12 @@ class EngineGPU {
   // phase and round.
   void setPersistent(bool on) { persistent_ = on; }
 
+  // CTAs per SM of the persistent run kernel (0 = as many as fit).
+  void setRunBlocksPerSM(int n) {
+    runBlocksPerSM_ = n > 0 ? n : 0;
+    runGrid_ = 0;
+  }
+
   // Round number handed to apply(v, g, round) by the stepwise API.
   void setIteration(int32_t it) { note(gas_core_set_iteration(core_, it)); }
 
@@ -170,6 +176,7 @@ class EngineGPU {
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &per, detail::run_persistent_kernel<Program>, detail::kGNT, 0);
+      if (self->runBlocksPerSM_ > 0 && self->runBlocksPerSM_ < per) per = self->runBlocksPerSM_;
       self->runGrid_ = (coop && per > 0 && sms > 0) ? per * sms : -1;
     }
     if (self->runGrid_ < 0) return GAS_ERR_UNSUPPORTED;
@@ -188,6 +195,7 @@ class EngineGPU {
   gas_status status_ = GAS_OK;
   bool persistent_ = true;
   int runGrid_ = 0;
+  int runBlocksPerSM_ = 0;
   VertexData *vdHost_ = nullptr;
   EdgeData *edHost_ = nullptr;
   int grid_ = 0;

@@ -35,6 +35,25 @@ extern "C" {
 #define GAS_DEVERR_TIMEOUT 1u    /* bounded look-back wait gave up */
 #define GAS_DEVERR_CAPACITY 2u   /* a queue would have overflowed  */
 
+/* Low-degree mode: when every vertex of a list has degree <= this bound,
+ * its phase runs one thread per vertex (edges folded left to right in CSC
+ * order) instead of merge-path tiles. */
+#define GAS_TPV_MAX_DEGREE 8
+#define GAS_TPV_TILE GAS_GATHER_THREADS
+
+/* A vertex list on the device: ids, exclusive prefix of the degree that the
+ * consumer walks (in-degree for the gather, out-degree for the scatter),
+ * CSC/CSR begin offset of each vertex, merge-path tile splits, and a
+ * control word pair (count << 32 | degree total, maximum degree). */
+typedef struct {
+  int32_t *vid;
+  int32_t *pre;
+  int32_t *beg;
+  int32_t *split;
+  unsigned long long *count;
+  unsigned int *maxDeg;
+} gas_vertex_list;
+
 /* Arguments of one gather+apply launch (device pointers). */
 typedef struct {
   /* graph: CSC for gather, CSR offsets for out-degrees */
@@ -53,20 +72,17 @@ typedef struct {
   int32_t rangeMode;
   int32_t rangeStart;
   int32_t rangeCount;
-  int32_t rangeBase;          /* inOffsets[rangeStart] */
-  const int32_t *frontVid;    /* list mode: vertex ids                    */
-  const int32_t *frontPre;    /* list mode: exclusive prefix of in-degree */
-  const unsigned long long *frontCount; /* list mode: (n << 32) | total in-edges */
-  const int32_t *frontSplit;  /* gather-tile merge-path splits            */
-  /* scatter list appended by this launch */
-  int32_t *scatVid;
-  int32_t *scatPre;
-  int32_t *scatSplit;
-  unsigned long long *scatCount;
-  int32_t capacity;           /* capacity of scatVid / frontVid lists     */
+  int32_t rangeBase;          /* inOffsets[rangeStart]                      */
+  int32_t rangeMaxDeg;        /* largest in-degree in the range (bound)     */
+  const int32_t *rangeSplit;  /* gather-tile splits of the range            */
+  gas_vertex_list front;      /* list mode                                  */
+  /* scatter list appended by this launch (out-degree prefix) */
+  gas_vertex_list scat;
+  int32_t capacity;           /* capacity of every vertex list              */
   int32_t maxScatTiles;
-  /* counters this launch resets for the following scatter */
+  /* list this launch resets for the following scatter (list mode) */
   unsigned long long *resetCount;
+  unsigned int *resetMaxDeg;
   unsigned int *resetTile;
   /* dynamic tile counter of this launch */
   unsigned int *tileCounter;
@@ -89,15 +105,8 @@ typedef struct {
   const int32_t *outDests;    /* CSR destinations [nEdges]                  */
   int32_t vertexBytes;
   int32_t maxGatherTiles;
-  int32_t *frontVid[2];
-  int32_t *frontPre[2];
-  int32_t *frontSplit[2];
-  int32_t *rangeSplit;
-  int32_t *scatVidB[2];
-  int32_t *scatPreB[2];
-  int32_t *scatSplitB[2];
-  unsigned long long *frontCnt[2];
-  unsigned long long *scatCnt[2];
+  gas_vertex_list frontL[2];  /* frontier lists (in-degree prefix)          */
+  gas_vertex_list scatL[2];   /* scatter lists (out-degree prefix)          */
   int32_t *mark;
   unsigned long long *stats;  /* 2 words per round, maxStatRounds rounds    */
   int32_t maxStatRounds;

@@ -26,6 +26,7 @@ struct EngineBase {
   virtual gas_status scatterActivate(bool s) = 0;
   virtual gas_status nextIter(int32_t *n) = 0;
   virtual gas_status run(int32_t maxIters, int32_t *iters) = 0;
+  virtual void setLaunch(bool persistent, int blocksPerSM) = 0;
 };
 
 template <class P>
@@ -66,6 +67,10 @@ struct BuiltinEngine final : EngineBase {
     int32_t it = eng.runFor(maxIters);
     if (iters) *iters = it;
     return eng.lastStatus();
+  }
+  void setLaunch(bool persistent, int blocksPerSM) override {
+    eng.setPersistent(persistent);
+    eng.setRunBlocksPerSM(blocksPerSM);
   }
 };
 
@@ -197,6 +202,14 @@ gas_status gas_engine_kernel_times(gas_engine *e, float *gatherMs, float *scatte
   GAS_ENGINE_CHECK(e);
   return gas_core_kernel_times(e->impl->core(), gatherMs, scatterMs, gatherLaunches,
                                scatterLaunches);
+}
+
+gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
+                                        int32_t runBlocksPerSM) {
+  GAS_ENGINE_CHECK(e);
+  if (runBlocksPerSM < 0) return fail(GAS_ERR_INVALID, "runBlocksPerSM must be >= 0");
+  e->impl->setLaunch(persistent != 0, runBlocksPerSM);
+  return GAS_OK;
 }
 
 gas_status gas_engine_last_run_ms(gas_engine *e, float *ms) {

@@ -79,9 +79,15 @@ using namespace gas::internal;
 
 namespace {
 
+struct ListCtl {
+  unsigned long long cnt;  // (count << 32) | degree total
+  unsigned maxd;           // largest degree in the list
+  unsigned pad;
+};
+
 struct Ctl {
-  unsigned long long fcnt[2];
-  unsigned long long scnt[2];
+  ListCtl f[2];  // frontier lists
+  ListCtl s[2];  // scatter lists
   unsigned tile[2];
   unsigned bar[2];  // persistent-kernel grid barrier: arrivals, generation
   int32_t rounds;   // rounds executed by the last persistent run
@@ -117,9 +123,12 @@ struct gas_core_s {
   void *ed = nullptr;
   void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr;
   int32_t *fvid[2] = {nullptr, nullptr}, *fpre[2] = {nullptr, nullptr};
+  int32_t *fbeg[2] = {nullptr, nullptr};
   int32_t *fsplit[2] = {nullptr, nullptr}, *rsplit = nullptr;
   int32_t *svid[2] = {nullptr, nullptr}, *spre[2] = {nullptr, nullptr};
+  int32_t *sbeg[2] = {nullptr, nullptr};
   int32_t *ssplit[2] = {nullptr, nullptr};
+  int32_t maxInDeg = 0;
   int32_t *mark = nullptr;
   void *carryVal = nullptr;
   unsigned *carryFlag = nullptr;
@@ -156,6 +165,7 @@ namespace {
 void free_graph(gas_core *c) {
   void *ptrs[] = {c->inOff, c->inSrc, c->outOff, c->outDst, c->ed, c->vd, c->vnew, c->vsaved,
                   c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
+                  c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
                   c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats};
   for (void *p : ptrs)
@@ -163,8 +173,8 @@ void free_graph(gas_core *c) {
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = nullptr;
   for (int k = 0; k < 2; ++k) {
-    c->fvid[k] = c->fpre[k] = c->fsplit[k] = nullptr;
-    c->svid[k] = c->spre[k] = c->ssplit[k] = nullptr;
+    c->fvid[k] = c->fpre[k] = c->fbeg[k] = c->fsplit[k] = nullptr;
+    c->svid[k] = c->spre[k] = c->sbeg[k] = c->ssplit[k] = nullptr;
   }
   c->rsplit = nullptr;
   c->mark = nullptr;
@@ -188,8 +198,8 @@ gas_status clean(gas_core *c, unsigned need) {
     unsigned bit;
     void *ptr;
     size_t bytes;
-  } m[] = {{kF0, &c->ctl->fcnt[0], 8}, {kF1, &c->ctl->fcnt[1], 8},
-           {kS0, &c->ctl->scnt[0], 8}, {kS1, &c->ctl->scnt[1], 8},
+  } m[] = {{kF0, &c->ctl->f[0], sizeof(ListCtl)}, {kF1, &c->ctl->f[1], sizeof(ListCtl)},
+           {kS0, &c->ctl->s[0], sizeof(ListCtl)}, {kS1, &c->ctl->s[1], sizeof(ListCtl)},
            {kT0, &c->ctl->tile[0], 4}, {kT1, &c->ctl->tile[1], 4}};
   for (auto &x : m)
     if (d & x.bit) {
@@ -202,6 +212,28 @@ gas_status clean(gas_core *c, unsigned need) {
 
 unsigned fbit(int k) { return k ? kF1 : kF0; }
 unsigned sbit(int k) { return k ? kS1 : kS0; }
+
+gas_vertex_list front_list(gas_core *c, int k) {
+  gas_vertex_list l;
+  l.vid = c->fvid[k];
+  l.pre = c->fpre[k];
+  l.beg = c->fbeg[k];
+  l.split = c->fsplit[k];
+  l.count = &c->ctl->f[k].cnt;
+  l.maxDeg = &c->ctl->f[k].maxd;
+  return l;
+}
+
+gas_vertex_list scat_list(gas_core *c, int k) {
+  gas_vertex_list l;
+  l.vid = c->svid[k];
+  l.pre = c->spre[k];
+  l.beg = c->sbeg[k];
+  l.split = c->ssplit[k];
+  l.count = &c->ctl->s[k].cnt;
+  l.maxDeg = &c->ctl->s[k].maxd;
+  return l;
+}
 
 gas_status check_device_error(gas_core *c) {
   unsigned err = 0;
@@ -308,6 +340,9 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
 
   c->nV = nV;
   c->nE = nE;
+  c->maxInDeg = 0;
+  for (int32_t v = 0; v < nV; ++v)
+    c->maxInDeg = std::max(c->maxInDeg, c->hInOff[(size_t)v + 1] - c->hInOff[v]);
   c->edgeBytes = edgeBytes;
   c->vertexBytes = vertexBytes;
   c->gatherBytes = gatherBytes;
@@ -328,6 +363,8 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   for (int k = 0; k < 2; ++k) {
     A(dalloc(&c->fvid[k], (size_t)nV));
     A(dalloc(&c->fpre[k], (size_t)nV));
+    A(dalloc(&c->fbeg[k], (size_t)nV));
+    A(dalloc(&c->sbeg[k], (size_t)nV));
     A(dalloc(&c->fsplit[k], (size_t)c->maxGatherTiles));
     A(dalloc(&c->svid[k], (size_t)nV));
     A(dalloc(&c->spre[k], (size_t)nV));
@@ -476,7 +513,7 @@ gas_status gas_core_count_active(gas_core *c, int32_t *n) {
   gas_status st = check_device_error(c);
   if (st) return st;
   unsigned long long v = 0;
-  cudaError_t e = cudaMemcpyAsync(&v, &c->ctl->fcnt[c->cur], 8, cudaMemcpyDeviceToHost,
+  cudaError_t e = cudaMemcpyAsync(&v, &c->ctl->f[c->cur].cnt, 8, cudaMemcpyDeviceToHost,
                                   c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "count_active");
@@ -518,17 +555,14 @@ gas_status gas_core_gather_apply(gas_core *c, int32_t haveGather, gas_gather_lau
   a.rangeStart = c->rstart;
   a.rangeCount = c->rcount;
   a.rangeBase = c->rangeMode ? c->hInOff[c->rstart] : 0;
-  a.frontVid = c->fvid[c->cur];
-  a.frontPre = c->fpre[c->cur];
-  a.frontCount = &c->ctl->fcnt[c->cur];
-  a.frontSplit = c->rangeMode ? c->rsplit : c->fsplit[c->cur];
-  a.scatVid = c->svid[c->sidx];
-  a.scatPre = c->spre[c->sidx];
-  a.scatSplit = c->ssplit[c->sidx];
-  a.scatCount = &c->ctl->scnt[c->sidx];
+  a.rangeMaxDeg = c->maxInDeg;
+  a.rangeSplit = c->rsplit;
+  a.front = front_list(c, c->cur);
+  a.scat = scat_list(c, c->sidx);
   a.capacity = c->nV;
   a.maxScatTiles = c->maxScatTiles;
-  a.resetCount = &c->ctl->fcnt[c->cur ^ 1];
+  a.resetCount = &c->ctl->f[c->cur ^ 1].cnt;
+  a.resetMaxDeg = &c->ctl->f[c->cur ^ 1].maxd;
   a.resetTile = &c->ctl->tile[1];
   a.tileCounter = &c->ctl->tile[0];
   a.carryVal = c->carryVal;
@@ -566,10 +600,7 @@ gas_status gas_core_scatter_activate(gas_core *c) {
   a.outOffsets = c->outOff;
   a.outDests = c->outDst;
   a.inOffsets = c->inOff;
-  a.scatVid = c->svid[c->sidx];
-  a.scatPre = c->spre[c->sidx];
-  a.scatSplit = c->ssplit[c->sidx];
-  a.scatCount = &c->ctl->scnt[c->sidx];
+  a.scat = scat_list(c, c->sidx);
   a.commit = c->pendingCommit ? 1 : 0;
   a.vertexBytes = c->vertexBytes;
   a.vertexData = c->vd;
@@ -578,18 +609,16 @@ gas_status gas_core_scatter_activate(gas_core *c) {
   a.rangeStart = c->rstart;
   a.rangeCount = c->rcount;
   a.frontVid = c->fvid[c->cur];
-  a.frontCount = &c->ctl->fcnt[c->cur];
-  a.nextVid = c->fvid[c->cur ^ 1];
-  a.nextPre = c->fpre[c->cur ^ 1];
-  a.nextSplit = c->fsplit[c->cur ^ 1];
-  a.nextCount = &c->ctl->fcnt[c->cur ^ 1];
+  a.frontCount = &c->ctl->f[c->cur].cnt;
+  a.next = front_list(c, c->cur ^ 1);
   a.maxGatherTiles = c->maxGatherTiles;
   a.capacity = c->nV;
   a.mark = c->mark;
   a.stamp = c->stamp;
   a.tileCounter = &c->ctl->tile[1];
   a.resetTile = &c->ctl->tile[0];
-  a.resetScatCount = &c->ctl->scnt[c->sidx ^ 1];
+  a.resetScatCount = &c->ctl->s[c->sidx ^ 1].cnt;
+  a.resetScatMaxDeg = &c->ctl->s[c->sidx ^ 1].maxd;
   a.errWord = &c->ctl->err;
   a.statSlot = c->round < kMaxRounds ? c->stats + 2 * (size_t)c->round : nullptr;
   gas::detail::scatter_activate_kernel<<<c->scatterGrid, gas::detail::kSNT, 0, c->stream>>>(a);
@@ -649,7 +678,7 @@ gas_status gas_core_run(gas_core *c, int32_t maxIters, int32_t haveGather,
     if ((st = gas_core_scatter_activate(c))) return st;
     if (pe) cudaEventRecord(pe[3], c->stream);
     if ((st = gas_core_next_iter(c))) return st;
-    cudaError_t e = cudaMemcpyAsync(&c->pinned[r % kRing], &c->ctl->fcnt[c->cur], 8,
+    cudaError_t e = cudaMemcpyAsync(&c->pinned[r % kRing], &c->ctl->f[c->cur].cnt, 8,
                                     cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(c->ev[r % kRing], c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "run bookkeeping");
@@ -715,8 +744,8 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
     A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
     c->stamp = 0;
   }
-  A(cudaMemsetAsync(&c->ctl->scnt[0], 0, sizeof(c->ctl->scnt), c->stream));
-  A(cudaMemsetAsync(&c->ctl->fcnt[c->cur ^ 1], 0, 8, c->stream));
+  A(cudaMemsetAsync(&c->ctl->s[0], 0, sizeof(c->ctl->s), c->stream));
+  A(cudaMemsetAsync(&c->ctl->f[c->cur ^ 1], 0, sizeof(ListCtl), c->stream));
   A(cudaMemsetAsync(&c->ctl->bar[0], 0, sizeof(c->ctl->bar) + sizeof(int32_t), c->stream));
   if (e != cudaSuccess) return cuda_fail(e, "run setup");
 
@@ -735,6 +764,8 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   a.rangeStart = c->rstart;
   a.rangeCount = c->rcount;
   a.rangeBase = c->rangeMode ? c->hInOff[c->rstart] : 0;
+  a.rangeMaxDeg = c->maxInDeg;
+  a.rangeSplit = c->rsplit;
   a.capacity = c->nV;
   a.maxScatTiles = c->maxScatTiles;
   a.carryVal = c->carryVal;
@@ -746,16 +777,9 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.vertexBytes = c->vertexBytes;
   ra.maxGatherTiles = c->maxGatherTiles;
   for (int k = 0; k < 2; ++k) {
-    ra.frontVid[k] = c->fvid[k];
-    ra.frontPre[k] = c->fpre[k];
-    ra.frontSplit[k] = c->fsplit[k];
-    ra.scatVidB[k] = c->svid[k];
-    ra.scatPreB[k] = c->spre[k];
-    ra.scatSplitB[k] = c->ssplit[k];
-    ra.frontCnt[k] = &c->ctl->fcnt[k];
-    ra.scatCnt[k] = &c->ctl->scnt[k];
+    ra.frontL[k] = front_list(c, k);
+    ra.scatL[k] = scat_list(c, k);
   }
-  ra.rangeSplit = c->rsplit;
   ra.mark = c->mark;
   ra.stats = c->stats + 2 * (size_t)std::min(c->round, kMaxRounds);
   ra.maxStatRounds = std::max(0, kMaxRounds - c->round);

@@ -126,6 +126,10 @@ class GASEngine:
     def restore_vertex_data(self) -> None:
         check(self._lib.gas_engine_restore_vertex_data(self._h), "gas_engine_restore_vertex_data")
 
+    def set_launch_config(self, persistent: bool = True, run_blocks_per_sm: int = 0) -> None:
+        check(self._lib.gas_engine_set_launch_config(self._h, int(persistent), run_blocks_per_sm),
+              "gas_engine_set_launch_config")
+
     def set_profiling(self, enabled: bool) -> None:
         check(self._lib.gas_engine_set_profiling(self._h, int(enabled)), "gas_engine_set_profiling")
 
