@@ -151,6 +151,29 @@ GAS_API gas_status gas_engine_kernel_times(gas_engine *e, float *gatherMs, float
 GAS_API gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
                                                 int32_t runBlocksPerSM);
 
+/* Breadth-first search that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- device memory
+ * already claimed by another allocator, or a serving thread that must not
+ * pay cudaMalloc's device synchronisation -- the graph and the result live
+ * in device memory the caller owns: outOffsets[nVertices+1] and
+ * outDests[nEdges] (CSR), depth[nVertices] (written: -1 unreached, else the
+ * round at which the vertex was reached, as bfs.cu:31-78).  All scratch is
+ * one fixed file-scope __device__ array (about 3.4 MB, held by every GPU
+ * that loads the library until exit), so graphs are limited to
+ * GAS_NOALLOC_MAX_VERTICES vertices and GAS_NOALLOC_MAX_EDGES edges; larger
+ * ones are rejected with GAS_ERR_INVALID.  The first call on a device looks
+ * up that array's device address, so make it before any stream capture.
+ * Every call reuses the same array: calls that overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller.
+ * Runs on `stream` (a cudaStream_t, NULL = legacy default stream) and
+ * returns when the search is done; *rounds (may be NULL) receives the
+ * number of rounds. */
+#define GAS_NOALLOC_MAX_VERTICES 65536
+#define GAS_NOALLOC_MAX_EDGES 2097152
+GAS_API gas_status gas_bfs_noalloc(int32_t nVertices, int32_t nEdges, const int32_t *outOffsets,
+                                   const int32_t *outDests, int32_t source, int32_t *depth,
+                                   void *stream, int32_t *rounds);
+
 /* ---------------- status / diagnostics ---------------------------------- */
 GAS_API const char *gas_status_string(gas_status s);
 GAS_API const char *gas_last_error(void);

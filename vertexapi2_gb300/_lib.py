@@ -67,6 +67,7 @@ SIGNATURES = {
     "gas_engine_set_profiling": (_I32, [_P, _I32]),
     "gas_engine_set_launch_config": (_I32, [_P, _I32, _I32]),
     "gas_engine_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
+    "gas_bfs_noalloc": (_I32, [_I32, _I32, _P, _P, _I32, _P, _P, _PI32]),
     # diagnostics
     "gas_status_string": (C.c_char_p, [_I32]),
     "gas_last_error": (C.c_char_p, []),
