@@ -90,7 +90,9 @@ GAS_API gas_status gas_engine_get_results(gas_engine *e);
  * the graph; the vertex-data half of setGraph (gpugas.h:221-226). */
 GAS_API gas_status gas_engine_set_vertex_data(gas_engine *e, const void *host);
 
-/* Replaces setActive (gpugas.h:342-349): active set = [start, end). */
+/* Replaces setActive (gpugas.h:342-349): active set = [start, end).
+ * Starts a new traversal: the round number handed to programs that take
+ * one (BFS depth) restarts at 0. */
 GAS_API gas_status gas_engine_set_active(gas_engine *e, int32_t vertexStart, int32_t vertexEnd);
 
 /* Replaces countActive (gpugas.h:353-356).  Waits for queued work. */

@@ -487,6 +487,7 @@ gas_status gas_core_set_active(gas_core *c, int32_t start, int32_t end) {
   c->haveScatList = false;
   c->countValid = false;
   c->round = 0;
+  c->iteration = 0;  // a new traversal: rounds (and BFS depths) count from 0
   const int32_t T = c->hInOff[end] - c->hInOff[start];
   const long long items = (long long)c->rcount + T;
   const int nsplit = (int)((items + GAS_GATHER_TILE - 1) / GAS_GATHER_TILE) + 1;
