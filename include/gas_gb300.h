@@ -153,6 +153,13 @@ GAS_API gas_status gas_engine_kernel_times(gas_engine *e, float *gatherMs, float
 GAS_API gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
                                                 int32_t runBlocksPerSM);
 
+/* Frontier policy of run(): a round runs dense -- one pull pass over every
+ * vertex's in-edges, the reference's dense path (gpugas.h:689-717) without
+ * its scan -- when the previous round's apply-returned-true vertices have
+ * more than nEdges/alpha out-edges (the reference switches at nEdges/100);
+ * 0 keeps every round on frontier lists.  Results do not depend on it. */
+GAS_API gas_status gas_engine_set_dense_policy(gas_engine *e, int32_t alpha);
+
 /* Breadth-first search that allocates nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc -- device memory
  * already claimed by another allocator, or a serving thread that must not

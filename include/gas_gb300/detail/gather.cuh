@@ -254,6 +254,7 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
   SegVal<GR> mine;
   mine.end = anyEnd;
   mine.has = has;
+  mine.act = 0u;
   mine.val = acc;
   SegVal<GR> excl, tot;
   block_seg_scan<P, GR, kGNT>(mine, excl, tot, sm.seg);
@@ -262,7 +263,7 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
   if (tid == kGNT - 1 && tot.has) {
     reinterpret_cast<GR *>(a.carryVal)[t] = tot.val;
     __threadfence();
-    st_release(a.carryFlag + t, a.epoch);
+    publish_flag(a.carryFlag + t, a.epoch, 0u);
   }
   // ---- look-back for a first vertex that started in an earlier tile
   const bool headSplit = nb > 0 && sm.headPre < j0;
@@ -276,8 +277,9 @@ __device__ void gather_tile(const gas_gather_args &a, int t, int n, int T, Gathe
         const int cnt = min(32, t - c0);
         unsigned h = 0u;
         GR x;
+        unsigned act;
         if (ti < t) {
-          if (wait_flag(a.carryFlag + ti, a.epoch, a.errWord)) {
+          if (wait_epoch(a.carryFlag + ti, a.epoch, a.errWord, &act)) {
             x = load_cg(reinterpret_cast<const GR *>(a.carryVal) + ti);
             h = 1u;
           }

@@ -9,6 +9,11 @@
 //   gather/apply tiles  -> grid barrier -> commit + scatter/activate tiles
 //   -> grid barrier -> swap frontier, next round
 //
+// Rounds whose predecessor activated many out-edges run dense (pull, see
+// dense.cuh): one pass and one barrier.  Transitions build the other
+// representation: list -> dense stamps the scatter list, dense -> list
+// compacts the stamped vertices into a scatter list and pushes it.
+//
 // Tiles are assigned statically (tile t to block t mod grid, in increasing
 // order per block); all blocks are co-resident (cooperative launch), so a
 // tile's look-back only waits on tiles that are being processed.  Every
@@ -16,6 +21,7 @@
 // GAS_DEVERR_TIMEOUT and the kernel returns.
 #pragma once
 
+#include "dense.cuh"
 #include "gather.cuh"
 #include "scatter.cuh"
 
@@ -63,19 +69,19 @@ template <class P>
 union PersistentSmem {
   GatherSmem<P> g;
   ScatterSmem s;
+  DenseSmem<P> d;
 };
 
 template <class P>
 __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args ra) {
+  enum { kList = 0, kDense = 1 };
   __shared__ PersistentSmem<P> sm;
   gas_gather_args a = ra.g;
   ScatterArgs sa;
   sa.outOffsets = a.outOffsets;
   sa.outDests = ra.outDests;
   sa.inOffsets = a.inOffsets;
-  sa.commit = a.haveGather;
   sa.vertexBytes = ra.vertexBytes;
-  sa.vertexData = a.vertexData;
   sa.vertexNew = a.vertexNew;
   sa.rangeStart = a.rangeStart;
   sa.rangeCount = a.rangeCount;
@@ -88,66 +94,153 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
   sa.resetScatMaxDeg = nullptr;
   sa.errWord = a.errWord;
   sa.statSlot = nullptr;
+  DenseCtx dc;
+  dc.nVertices = a.nVertices;
+  dc.nEdges = a.nEdges;
+  dc.inOffsets = a.inOffsets;
+  dc.inSources = a.inSources;
+  dc.outOffsets = a.outOffsets;
+  dc.edgeData = a.edgeData;
+  dc.split = ra.fullSplit;
+  dc.retStamp = ra.retStamp;
+  dc.haveGather = a.haveGather;
+  dc.carryVal = a.carryVal;
+  dc.carryFlag = a.carryFlag;
+  dc.errWord = a.errWord;
+  void *vdBuf[2] = {a.vertexData, ra.vertexAlt};
+  const long long E = a.nEdges;
 
-  int cur = ra.cur, sidx = ra.sidx;
+  int cur = ra.cur, sidx = ra.sidx, vcur = 0;
   bool rangeMode = a.rangeMode != 0;
+  int mode = ra.allActive ? kDense : kList;
+  bool allActive = ra.allActive != 0;
   int r = 0;
-  for (;; ++r) {
+  for (;;) {
     if (ra.maxRounds > 0 && r >= ra.maxRounds) break;
-    // ---- this round's frontier (final since the previous barrier)
-    a.rangeMode = rangeMode ? 1 : 0;
-    a.front = ra.frontL[cur];
-    a.scat = ra.scatL[sidx];
-    a.epoch = ra.epochBase + (unsigned)r;
-    a.iteration = ra.g.iteration + r;
-    int n, T;
-    frontier_size(a, n, T);
-    if (n == 0) break;  // uniform: every block read the same count
+    const unsigned epoch = ra.epochBase + (unsigned)r;
+    const int32_t stamp = ra.stampBase + r;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       *ra.frontL[cur ^ 1].count = 0ull;  // appended by this round's scatter
       *ra.frontL[cur ^ 1].maxDeg = 0u;
       *ra.scatL[sidx ^ 1].count = 0ull;  // appended by the next round's gather
       *ra.scatL[sidx ^ 1].maxDeg = 0u;
+      unsigned long long *nextCnt = ra.denseCnt + 2 * ((r + 1) % 3);
+      nextCnt[0] = 0ull;
+      nextCnt[1] = 0ull;
     }
-    // ---- gather/apply
-    bool tpvG;
-    const int ntG = gather_tiles(a, n, T, tpvG);
-    for (int t = blockIdx.x; t < ntG; t += gridDim.x) {
-      gather_dispatch<P>(a, t, n, T, tpvG, sm.g);
-      __syncthreads();
+    unsigned long long statA, statR;
+    bool denseNext;
+    if (mode == kList) {
+      // ---------------- push round: list (or range) frontier
+      a.rangeMode = rangeMode ? 1 : 0;
+      a.front = ra.frontL[cur];
+      a.scat = ra.scatL[sidx];
+      a.epoch = epoch;
+      a.iteration = ra.g.iteration + r;
+      a.vertexData = vdBuf[vcur];
+      int n, T;
+      frontier_size(a, n, T);
+      if (n == 0) break;  // uniform: every block read the same count
+      bool tpvG;
+      const int ntG = gather_tiles(a, n, T, tpvG);
+      for (int t = blockIdx.x; t < ntG; t += gridDim.x) {
+        gather_dispatch<P>(a, t, n, T, tpvG, sm.g);
+        __syncthreads();
+      }
+      if (!grid_barrier(ra.barrier, a.errWord)) break;
+      const unsigned long long sc = *a.scat.count;
+      int ns = (int)(sc >> 32);
+      if (ns > a.capacity) ns = a.capacity;
+      const int Ts = (int)(sc & 0xffffffffull);
+      statA = ((unsigned long long)n << 32) | (unsigned)T;
+      statR = sc;
+      denseNext = ra.denseAlpha > 0 && ns > 0 && (long long)Ts * ra.denseAlpha > E;
+      sa.commit = a.haveGather;
+      sa.vertexData = vdBuf[vcur];
+      sa.scat = a.scat;
+      sa.rangeMode = a.rangeMode;
+      sa.frontVid = a.front.vid;
+      sa.frontCount = a.front.count;
+      sa.next = ra.frontL[cur ^ 1];
+      sa.stamp = stamp;
+      if (a.haveGather) commit_frontier(sa, n);
+      if (denseNext) {
+        stamp_list(a.scat, ns, ra.retStamp, stamp);
+      } else {
+        bool tpvS;
+        const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
+        for (int t = blockIdx.x; t < ntS; t += gridDim.x) {
+          if (tpvS)
+            tpv_scatter_tile(sa, t, ns, Ts, sm.s);
+          else
+            scatter_tile(sa, t, ns, Ts, sm.s);
+          __syncthreads();
+        }
+      }
+      if (!grid_barrier(ra.barrier, a.errWord)) break;
+    } else {
+      // ---------------- pull round over every vertex
+      dc.vdCur = vdBuf[vcur];
+      dc.vdNext = vdBuf[vcur ^ 1];
+      dc.prevStamp = stamp - 1;
+      dc.curStamp = stamp;
+      dc.allActive = allActive ? 1 : 0;
+      dc.epoch = epoch;
+      dc.iteration = ra.g.iteration + r;
+      dc.cnt = ra.denseCnt + 2 * (r % 3);
+      const int ntD = (int)(((long long)a.nVertices + a.nEdges + kGTILE - 1) / kGTILE);
+      for (int t = blockIdx.x; t < ntD; t += gridDim.x) {
+        dense_tile<P>(dc, t, sm.d);
+        __syncthreads();
+      }
+      if (!grid_barrier(ra.barrier, a.errWord)) break;
+      statA = dc.cnt[0];
+      statR = dc.cnt[1];
+      if ((statA >> 32) == 0) break;  // no vertex was active: the run ended before this round
+      vcur ^= 1;
+      const int nr = (int)(statR >> 32);
+      const long long eout = (long long)(statR & 0xffffffffull);
+      denseNext = ra.denseAlpha > 0 && nr > 0 && eout * ra.denseAlpha > E;
+      if (!denseNext && nr > 0) {
+        // dense -> list: compact the stamped vertices, then push them
+        compact_ret<kGNT, kGVT>(ra.retStamp, stamp, a.outOffsets, a.nVertices, ra.scatL[sidx],
+                                a.maxScatTiles, a.errWord, sm.g.app);
+        if (!grid_barrier(ra.barrier, a.errWord)) break;
+        const unsigned long long sc = *ra.scatL[sidx].count;
+        int ns = (int)(sc >> 32);
+        if (ns > a.capacity) ns = a.capacity;
+        const int Ts = (int)(sc & 0xffffffffull);
+        sa.commit = 0;
+        sa.scat = ra.scatL[sidx];
+        sa.next = ra.frontL[cur ^ 1];
+        sa.stamp = stamp;
+        bool tpvS;
+        const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
+        for (int t = blockIdx.x; t < ntS; t += gridDim.x) {
+          if (tpvS)
+            tpv_scatter_tile(sa, t, ns, Ts, sm.s);
+          else
+            scatter_tile(sa, t, ns, Ts, sm.s);
+          __syncthreads();
+        }
+        if (!grid_barrier(ra.barrier, a.errWord)) break;
+      }
     }
-    if (!grid_barrier(ra.barrier, a.errWord)) break;
-    // ---- commit + scatter/activate
-    sa.scat = a.scat;
-    sa.rangeMode = a.rangeMode;
-    sa.frontVid = a.front.vid;
-    sa.frontCount = a.front.count;
-    sa.next = ra.frontL[cur ^ 1];
-    sa.stamp = ra.stampBase + r;
-    const unsigned long long sc = *a.scat.count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && r < ra.maxStatRounds) {
-      ra.stats[2 * (size_t)r] = ((unsigned long long)n << 32) | (unsigned)T;
-      ra.stats[2 * (size_t)r + 1] = sc;
+      ra.stats[2 * (size_t)r] = statA;
+      ra.stats[2 * (size_t)r + 1] = statR;
     }
-    if (a.haveGather) commit_frontier(sa, n);
-    int ns = (int)(sc >> 32);
-    if (ns > a.capacity) ns = a.capacity;
-    const int Ts = (int)(sc & 0xffffffffull);
-    bool tpvS;
-    const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
-    for (int t = blockIdx.x; t < ntS; t += gridDim.x) {
-      if (tpvS)
-        tpv_scatter_tile(sa, t, ns, Ts, sm.s);
-      else
-        scatter_tile(sa, t, ns, Ts, sm.s);
-      __syncthreads();
-    }
-    if (!grid_barrier(ra.barrier, a.errWord)) break;
+    ++r;
+    mode = denseNext ? kDense : kList;
+    allActive = false;
+    rangeMode = false;
     cur ^= 1;
     sidx ^= 1;
-    rangeMode = false;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) *ra.roundsOut = r;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *ra.roundsOut = r;
+    if (ra.vcurOut) *ra.vcurOut = vcur;
+  }
 }
 
 }  // namespace detail

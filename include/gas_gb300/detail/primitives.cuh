@@ -83,17 +83,27 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Waits (bounded) until *flag == want.  Returns false and sets
-// GAS_DEVERR_TIMEOUT in *err when the limit is reached.
-__device__ __forceinline__ bool wait_flag(const unsigned *flag, unsigned want, unsigned *err) {
+// Tile aggregates are published with flag = (epoch << 1) | act.
+__device__ __forceinline__ void publish_flag(unsigned *flag, unsigned epoch, unsigned act) {
+  st_release(flag, (epoch << 1) | (act & 1u));
+}
+
+// Waits (bounded) until *flag carries `epoch`; returns false and sets
+// GAS_DEVERR_TIMEOUT in *err when the limit is reached.  *act receives the
+// published activation bit.
+__device__ __forceinline__ bool wait_epoch(const unsigned *flag, unsigned epoch, unsigned *err,
+                                           unsigned *act) {
   unsigned spins = 0;
-  while (ld_acquire(flag) != want) {
+  unsigned f;
+  while (((f = ld_acquire(flag)) >> 1) != epoch) {
     if (++spins > kSpinLimit) {
       atomicOr(err, GAS_DEVERR_TIMEOUT);
+      *act = 0u;
       return false;
     }
     __nanosleep(64);
   }
+  *act = f & 1u;
   return true;
 }
 
@@ -139,11 +149,13 @@ __device__ __forceinline__ void block_exclusive_scan_u64(unsigned long long x,
 // ---------------------------------------------------------------------------
 // Segmented partial reductions.  A SegVal is the state flowing between
 // consecutive items: `end` = a vertex boundary occurred inside, `has` = val
-// holds a reduction of at least one gathered edge value.
+// holds a reduction of at least one gathered edge value, `act` = one of
+// those edges activates its destination (dense rounds).
 template <typename T>
 struct SegVal {
   unsigned end;
   unsigned has;
+  unsigned act;
   T val;
 };
 
@@ -152,6 +164,7 @@ __device__ __forceinline__ SegVal<T> seg_combine(const SegVal<T> &a, const SegVa
   if (b.end) return b;
   SegVal<T> r;
   r.end = a.end;
+  r.act = a.act | b.act;
   if (!a.has) {
     r.has = b.has;
     r.val = b.val;
@@ -182,6 +195,7 @@ __device__ __forceinline__ void block_seg_scan(const SegVal<T> &x, SegVal<T> &ex
     SegVal<T> o;
     o.end = __shfl_up_sync(kFullMask, incl.end, d);
     o.has = __shfl_up_sync(kFullMask, incl.has, d);
+    o.act = __shfl_up_sync(kFullMask, incl.act, d);
     o.val = shfl_up_any(incl.val, d);
     if (lane >= d) incl = seg_combine<P>(o, incl);
   }
@@ -194,12 +208,14 @@ __device__ __forceinline__ void block_seg_scan(const SegVal<T> &x, SegVal<T> &ex
     } else {
       w.end = 0u;
       w.has = 0u;
+      w.act = 0u;
     }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       SegVal<T> o;
       o.end = __shfl_up_sync(kFullMask, w.end, d);
       o.has = __shfl_up_sync(kFullMask, w.has, d);
+      o.act = __shfl_up_sync(kFullMask, w.act, d);
       o.val = shfl_up_any(w.val, d);
       if (lane >= d) w = seg_combine<P>(o, w);
     }
@@ -212,10 +228,12 @@ __device__ __forceinline__ void block_seg_scan(const SegVal<T> &x, SegVal<T> &ex
   } else {
     wpre.end = 0u;
     wpre.has = 0u;
+    wpre.act = 0u;
   }
   SegVal<T> prev;
   prev.end = __shfl_up_sync(kFullMask, incl.end, 1);
   prev.has = __shfl_up_sync(kFullMask, incl.has, 1);
+  prev.act = __shfl_up_sync(kFullMask, incl.act, 1);
   prev.val = shfl_up_any(incl.val, 1);
   if (lane == 0) {
     excl = wpre;

@@ -117,6 +117,14 @@ typedef struct {
   int32_t stampBase;          /* activation stamp of round 0                */
   unsigned *barrier;          /* [2]: arrival count, generation             */
   int32_t *roundsOut;         /* rounds executed                            */
+  /* dense (pull) rounds */
+  void *vertexAlt;            /* second vertex-data buffer (ping-pong)      */
+  int32_t *retStamp;          /* [V] stamp of the round whose apply returned true */
+  const int32_t *fullSplit;   /* gather-tile splits of [0, V)               */
+  unsigned long long *denseCnt; /* [3][2] per-round counters                */
+  int32_t denseAlpha;         /* next round dense when out-edges*alpha > E; 0 = never */
+  int32_t allActive;          /* round 0 is every vertex (setActive(0, V)) */
+  int32_t *vcurOut;           /* 1 when the final vertex data is in vertexAlt */
 } gas_run_args;
 
 typedef struct gas_core_s gas_core;
@@ -182,6 +190,10 @@ GAS_API gas_status gas_core_last_run_ms(gas_core *c, float *ms);
 GAS_API gas_status gas_core_save_vertex_data(gas_core *c);
 GAS_API gas_status gas_core_restore_vertex_data(gas_core *c);
 GAS_API gas_status gas_core_set_profiling(gas_core *c, int32_t enabled);
+/* run(): a round runs dense (pull over every vertex) when the previous
+ * round's apply-returned-true vertices have more than nEdges/alpha
+ * out-edges; 0 disables dense rounds.  Results do not depend on it. */
+GAS_API gas_status gas_core_set_dense_policy(gas_core *c, int32_t alpha);
 GAS_API gas_status gas_core_kernel_times(gas_core *c, float *gatherMs, float *scatterMs,
                                          int32_t *gatherLaunches, int32_t *scatterLaunches);
 /* Waits for queued work and reports device-side errors. */

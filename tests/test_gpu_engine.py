@@ -274,3 +274,54 @@ def test_c2_sssp_grid_full_size(gpu, port):
     assert rounds == st["iterations"]
     assert np.array_equal(gst["active"], st["active"])
     assert np.array_equal(gst["gathered"], st["gathered"])
+
+
+def _run_policy(program, nv, s, d, init, w=None, active=None, alpha=10, max_iters=0):
+    vd = init.copy()
+    with GASEngine(program) as e:
+        e.set_graph(nv, vd, s, d, w)
+        e.set_dense_policy(alpha)
+        lo, hi = active if active else (0, nv)
+        e.set_active(lo, hi)
+        rounds = e.run(max_iters)
+        st = e.round_stats()
+        e.get_results()
+    return vd, rounds, st
+
+
+@pytest.mark.parametrize("alpha", [0, 10, 1000])
+def test_dense_policy_does_not_change_results(gpu, port, alpha):
+    """Dense (pull) rounds, list (push) rounds and every mix of the two give
+    identical results and identical per-round frontier counts."""
+    g = graphs.rmat(14, 16, seed=31, symmetrize=True, weights=(1, 255))
+    nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
+    src = P.max_outdegree_vertex(nv, s)
+    ref, st = port.bfs(nv, s, d, src, stats_cap=256)
+    got, rounds, gst = _run_policy(PROGRAM_BFS, nv, s, d, P.bfs_init(nv), active=(src, src + 1),
+                                   alpha=alpha)
+    assert np.array_equal(got, ref) and rounds == st["iterations"]
+    for k in ("active", "gathered", "ret", "scattered"):
+        assert np.array_equal(gst[k], st[k]), k
+    ref, st = port.cc(nv, s, d, stats_cap=256)
+    got, rounds, gst = _run_policy(PROGRAM_CC, nv, s, d, P.cc_init(nv), alpha=alpha)
+    assert np.array_equal(got, ref) and rounds == st["iterations"]
+    assert np.array_equal(gst["active"], st["active"])
+    ref, st = port.sssp(nv, s, d, w, 0, stats_cap=4096)
+    got, rounds, gst = _run_policy(PROGRAM_SSSP, nv, s, d, P.sssp_init(nv, 0), w=w, alpha=alpha)
+    assert np.array_equal(got, ref) and rounds == st["iterations"]
+    assert np.array_equal(gst["gathered"], st["gathered"])
+    gd = graphs.rmat(14, 16, seed=32)
+    ref64, st = port.pagerank(gd.n_vertices, gd.srcs, gd.dsts, max_iters=50, fp64=True)
+    got, rounds, _ = _run_policy(PROGRAM_PAGERANK, gd.n_vertices, gd.srcs, gd.dsts,
+                                 P.pagerank_init(gd.n_vertices, gd.srcs), alpha=alpha,
+                                 max_iters=50)
+    assert rel_l1(got["rank"], ref64) <= PR_REL_L1
+
+
+def test_dense_rounds_are_deterministic(gpu):
+    """With every round dense the FP32 PageRank is bit-identical run to run."""
+    gd = graphs.rmat(15, 16, seed=33)
+    runs = [_run_policy(PROGRAM_PAGERANK, gd.n_vertices, gd.srcs, gd.dsts,
+                        P.pagerank_init(gd.n_vertices, gd.srcs), alpha=1 << 20, max_iters=30)[0]
+            for _ in range(2)]
+    assert np.array_equal(runs[0]["rank"], runs[1]["rank"])

@@ -66,6 +66,7 @@ SIGNATURES = {
     "gas_engine_restore_vertex_data": (_I32, [_P]),
     "gas_engine_set_profiling": (_I32, [_P, _I32]),
     "gas_engine_set_launch_config": (_I32, [_P, _I32, _I32]),
+    "gas_engine_set_dense_policy": (_I32, [_P, _I32]),
     "gas_engine_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
     "gas_bfs_noalloc": (_I32, [_I32, _I32, _P, _P, _I32, _P, _P, _PI32]),
     # diagnostics
@@ -100,6 +101,7 @@ SIGNATURES = {
     "gas_core_save_vertex_data": (_I32, [_P]),
     "gas_core_restore_vertex_data": (_I32, [_P]),
     "gas_core_set_profiling": (_I32, [_P, _I32]),
+    "gas_core_set_dense_policy": (_I32, [_P, _I32]),
     "gas_core_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
 }
 

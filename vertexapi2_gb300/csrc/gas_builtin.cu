@@ -212,6 +212,11 @@ gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
   return GAS_OK;
 }
 
+gas_status gas_engine_set_dense_policy(gas_engine *e, int32_t alpha) {
+  GAS_ENGINE_CHECK(e);
+  return gas_core_set_dense_policy(e->impl->core(), alpha);
+}
+
 gas_status gas_engine_last_run_ms(gas_engine *e, float *ms) {
   GAS_ENGINE_CHECK(e);
   return gas_core_last_run_ms(e->impl->core(), ms);

@@ -91,7 +91,10 @@ struct Ctl {
   unsigned tile[2];
   unsigned bar[2];  // persistent-kernel grid barrier: arrivals, generation
   int32_t rounds;   // rounds executed by the last persistent run
+  int32_t vcur;     // 1 when that run's result is in the alternate buffer
+  unsigned long long dense[3][2];  // per-round counters of dense rounds
   unsigned err;     // device error bits (kept across set_active)
+  unsigned pad;
 };
 
 enum DirtyBit : unsigned {
@@ -121,7 +124,9 @@ struct gas_core_s {
   std::vector<int32_t> hInOff, hOutOff, cscPerm;
   int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
   void *ed = nullptr;
-  void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr;
+  void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr, *valt = nullptr;
+  int32_t *retStamp = nullptr, *fullSplit = nullptr;
+  int32_t denseAlpha = 10;  // dense (pull) round when out-edges * alpha > E
   int32_t *fvid[2] = {nullptr, nullptr}, *fpre[2] = {nullptr, nullptr};
   int32_t *fbeg[2] = {nullptr, nullptr};
   int32_t *fsplit[2] = {nullptr, nullptr}, *rsplit = nullptr;
@@ -164,6 +169,7 @@ namespace {
 
 void free_graph(gas_core *c) {
   void *ptrs[] = {c->inOff, c->inSrc, c->outOff, c->outDst, c->ed, c->vd, c->vnew, c->vsaved,
+                  c->valt, c->retStamp, c->fullSplit,
                   c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
@@ -171,7 +177,8 @@ void free_graph(gas_core *c) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
-  c->ed = c->vd = c->vnew = c->vsaved = nullptr;
+  c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
+  c->retStamp = c->fullSplit = nullptr;
   for (int k = 0; k < 2; ++k) {
     c->fvid[k] = c->fpre[k] = c->fbeg[k] = c->fsplit[k] = nullptr;
     c->svid[k] = c->spre[k] = c->sbeg[k] = c->ssplit[k] = nullptr;
@@ -360,6 +367,9 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   if (edgeBytes > 0) A(cudaMalloc(&c->ed, (size_t)edgeBytes * std::max(nE, 1)));
   A(cudaMalloc(&c->vd, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->vnew, (size_t)vertexBytes * std::max(nV, 1)));
+  A(cudaMalloc(&c->valt, (size_t)vertexBytes * std::max(nV, 1)));
+  A(dalloc(&c->retStamp, (size_t)nV));
+  A(dalloc(&c->fullSplit, (size_t)c->maxGatherTiles));
   for (int k = 0; k < 2; ++k) {
     A(dalloc(&c->fvid[k], (size_t)nV));
     A(dalloc(&c->fpre[k], (size_t)nV));
@@ -402,6 +412,13 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
                       c->stream));
   }
   A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
+  A(cudaMemsetAsync(c->retStamp, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
+  if (nV > 0) {
+    const int nsplit = (int)(((long long)nV + nE + GAS_GATHER_TILE - 1) / GAS_GATHER_TILE) + 1;
+    gas::detail::range_split_kernel<<<(nsplit + 127) / 128, 128, 0, c->stream>>>(
+        c->inOff, 0, nV, nE, c->fullSplit, nsplit);
+    A(cudaGetLastError());
+  }
   A(cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream));
   A(cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream));
   A(cudaMemsetAsync(c->vd, 0, (size_t)vertexBytes * std::max(nV, 1), c->stream));
@@ -538,7 +555,7 @@ gas_status gas_core_gather_apply(gas_core *c, int32_t haveGather, gas_gather_lau
   if (st) return st;
   st = clean(c, sbit(c->sidx) | kT0);
   if (st) return st;
-  if (++c->epoch == 0xffffffffu) {
+  if (++c->epoch >= 0x7fffffffu) {  // flags hold epoch << 1
     cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream);
     c->epoch = 1;
   }
@@ -737,14 +754,16 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   auto A = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
   };
-  if (c->epoch > 0xC0000000u) {
+  if (c->epoch > 0x40000000u) {  // flags hold epoch << 1
     A(cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream));
     c->epoch = 0;
   }
   if (c->stamp > 0x40000000) {
     A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
+    A(cudaMemsetAsync(c->retStamp, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
     c->stamp = 0;
   }
+  A(cudaMemsetAsync(&c->ctl->dense[0][0], 0, sizeof(c->ctl->dense), c->stream));
   A(cudaMemsetAsync(&c->ctl->s[0], 0, sizeof(c->ctl->s), c->stream));
   A(cudaMemsetAsync(&c->ctl->f[c->cur ^ 1], 0, sizeof(ListCtl), c->stream));
   A(cudaMemsetAsync(&c->ctl->bar[0], 0, sizeof(c->ctl->bar) + sizeof(int32_t), c->stream));
@@ -791,6 +810,13 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.stampBase = c->stamp + 1;
   ra.barrier = &c->ctl->bar[0];
   ra.roundsOut = &c->ctl->rounds;
+  ra.vertexAlt = c->valt;
+  ra.retStamp = c->retStamp;
+  ra.fullSplit = c->fullSplit;
+  ra.denseCnt = &c->ctl->dense[0][0];
+  ra.denseAlpha = c->denseAlpha;
+  ra.allActive = (c->rangeMode && c->rstart == 0 && c->rcount == c->nV && c->denseAlpha > 0) ? 1 : 0;
+  ra.vcurOut = &c->ctl->vcur;
 
   cudaEventRecord(c->t0, c->stream);
   st = runLaunch(user, &ra, (void *)c->stream);
@@ -799,10 +825,17 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "persistent run launch");
   cudaEventRecord(c->t1, c->stream);
-  int32_t rounds = 0;
-  A(cudaMemcpyAsync(&rounds, &c->ctl->rounds, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  int32_t rv[2] = {0, 0};  // rounds, vcur (adjacent in Ctl)
+  A(cudaMemcpyAsync(rv, &c->ctl->rounds, sizeof(rv), cudaMemcpyDeviceToHost, c->stream));
   A(cudaStreamSynchronize(c->stream));
   if (e != cudaSuccess) return cuda_fail(e, "persistent run");
+  const int32_t rounds = rv[0];
+  if (rv[1]) {  // the result ended in the alternate buffer of the dense rounds
+    A(cudaMemcpyAsync(c->vd, c->valt, (size_t)c->vertexBytes * c->nV, cudaMemcpyDeviceToDevice,
+                      c->stream));
+    A(cudaStreamSynchronize(c->stream));
+    if (e != cudaSuccess) return cuda_fail(e, "persistent run copy-back");
+  }
   cudaEventElapsedTime(&c->lastMs, c->t0, c->t1);
   const int32_t R = rounds;
   if (R & 1) {
@@ -873,6 +906,13 @@ gas_status gas_core_restore_vertex_data(gas_core *c) {
   const size_t bytes = (size_t)c->vertexBytes * std::max(c->nV, 1);
   cudaError_t e = cudaMemcpyAsync(c->vd, c->vsaved, bytes, cudaMemcpyDeviceToDevice, c->stream);
   return e == cudaSuccess ? GAS_OK : cuda_fail(e, "restore_vertex_data");
+}
+
+gas_status gas_core_set_dense_policy(gas_core *c, int32_t alpha) {
+  if (!c) return fail(GAS_ERR_INVALID, "set_dense_policy: engine is NULL");
+  if (alpha < 0) return fail(GAS_ERR_INVALID, "dense policy alpha must be >= 0");
+  c->denseAlpha = alpha;
+  return GAS_OK;
 }
 
 gas_status gas_core_set_profiling(gas_core *c, int32_t enabled) {

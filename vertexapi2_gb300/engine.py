@@ -130,6 +130,9 @@ class GASEngine:
         check(self._lib.gas_engine_set_launch_config(self._h, int(persistent), run_blocks_per_sm),
               "gas_engine_set_launch_config")
 
+    def set_dense_policy(self, alpha: int) -> None:
+        check(self._lib.gas_engine_set_dense_policy(self._h, alpha), "gas_engine_set_dense_policy")
+
     def set_profiling(self, enabled: bool) -> None:
         check(self._lib.gas_engine_set_profiling(self._h, int(enabled)), "gas_engine_set_profiling")
 
