@@ -248,7 +248,7 @@ __device__ void dense_tile(const DenseCtx &a, int t, DenseSmem<P> &sm) {
       const int m = vloc[v];
       const int vx = i0 + m;
       VD tmp = vd[vx];
-      if (segAct[v]) {
+      if (a.allActive || segAct[v]) {  // with every vertex active, in-degree 0 too
         GR g = gz;
         if (a.haveGather && segHas[v]) g = P::gatherReduce(gz, segVal[v]);
         const bool r = do_apply<P>(&tmp, g, a.iteration);
