@@ -7,7 +7,10 @@
 // gpugas.h:690-717, primitives/scatter_if_mgpu.h:130-157):
 //
 //   vertex v is active in round r+1  <=>  some in-neighbour u of v returned
-//   true in round r  (retStamp[u] == stamp of round r)
+//   true in round r  (retStamp[r & 1][u] == stamp of round r)
+//
+// The stamps of consecutive rounds live in two arrays, so a round reads the
+// previous round's set while it records its own.
 //
 // which is exactly the set the reference's scatterActivate builds, so the
 // active sets and round counts are unchanged.  The pass walks the whole CSC
@@ -33,8 +36,9 @@ struct DenseCtx {
   const int32_t *split;  // gather-tile splits of [0, nVertices)
   const void *vdCur;
   void *vdNext;
-  int32_t *retStamp;
-  int32_t prevStamp;     // stamp of the previous round's apply-returned-true set
+  const int32_t *prevRet;  // stamps written by the previous round (read only here)
+  int32_t *curRet;         // stamps of this round (the other array of the pair)
+  int32_t prevStamp;       // stamp of the previous round's apply-returned-true set
   int32_t curStamp;
   int32_t allActive;     // every vertex active (setActive(0, V))
   int32_t haveGather;
@@ -113,7 +117,7 @@ __device__ void dense_tile(const DenseCtx &a, int t, DenseSmem<P> &sm) {
   unsigned eact[kGVT];
 #pragma unroll
   for (int v = 0; v < kGVT; ++v)
-    eact[v] = (kind[v] == 1) && (a.allActive || a.retStamp[src[v]] == a.prevStamp) ? 1u : 0u;
+    eact[v] = (kind[v] == 1) && (a.allActive || a.prevRet[src[v]] == a.prevStamp) ? 1u : 0u;
   const GR gz = P::gatherZero;
   GR val[kGVT];
 #pragma unroll
@@ -256,7 +260,7 @@ __device__ void dense_tile(const DenseCtx &a, int t, DenseSmem<P> &sm) {
         ++nA;
         nEin += (unsigned)(sm.end[m] - start);
         if (r) {
-          a.retStamp[vx] = a.curStamp;
+          a.curRet[vx] = a.curStamp;
           ++nR;
           nEout += (unsigned)(a.outOffsets[vx + 1] - a.outOffsets[vx]);
         }

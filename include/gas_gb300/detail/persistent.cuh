@@ -102,7 +102,6 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
   dc.outOffsets = a.outOffsets;
   dc.edgeData = a.edgeData;
   dc.split = ra.fullSplit;
-  dc.retStamp = ra.retStamp;
   dc.haveGather = a.haveGather;
   dc.carryVal = a.carryVal;
   dc.carryFlag = a.carryFlag;
@@ -165,7 +164,7 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
       sa.stamp = stamp;
       if (a.haveGather) commit_frontier(sa, n);
       if (denseNext) {
-        stamp_list(a.scat, ns, ra.retStamp, stamp);
+        stamp_list(a.scat, ns, ra.retStamp[r & 1], stamp);
       } else {
         bool tpvS;
         const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
@@ -182,6 +181,8 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
       // ---------------- pull round over every vertex
       dc.vdCur = vdBuf[vcur];
       dc.vdNext = vdBuf[vcur ^ 1];
+      dc.prevRet = ra.retStamp[(r + 1) & 1];
+      dc.curRet = ra.retStamp[r & 1];
       dc.prevStamp = stamp - 1;
       dc.curStamp = stamp;
       dc.allActive = allActive ? 1 : 0;
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
       denseNext = ra.denseAlpha > 0 && nr > 0 && eout * ra.denseAlpha > E;
       if (!denseNext && nr > 0) {
         // dense -> list: compact the stamped vertices, then push them
-        compact_ret<kGNT, kGVT>(ra.retStamp, stamp, a.outOffsets, a.nVertices, ra.scatL[sidx],
+        compact_ret<kGNT, kGVT>(ra.retStamp[r & 1], stamp, a.outOffsets, a.nVertices, ra.scatL[sidx],
                                 a.maxScatTiles, a.errWord, sm.g.app);
         if (!grid_barrier(ra.barrier, a.errWord)) break;
         const unsigned long long sc = *ra.scatL[sidx].count;

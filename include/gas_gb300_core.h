@@ -119,7 +119,8 @@ typedef struct {
   int32_t *roundsOut;         /* rounds executed                            */
   /* dense (pull) rounds */
   void *vertexAlt;            /* second vertex-data buffer (ping-pong)      */
-  int32_t *retStamp;          /* [V] stamp of the round whose apply returned true */
+  int32_t *retStamp[2];       /* [V] each: stamp of the round whose apply returned
+                                 true; round r writes [r & 1] and reads [(r-1) & 1] */
   const int32_t *fullSplit;   /* gather-tile splits of [0, V)               */
   unsigned long long *denseCnt; /* [3][2] per-round counters                */
   int32_t denseAlpha;         /* next round dense when out-edges*alpha > E; 0 = never */

@@ -125,7 +125,7 @@ struct gas_core_s {
   int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
   void *ed = nullptr;
   void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr, *valt = nullptr;
-  int32_t *retStamp = nullptr, *fullSplit = nullptr;
+  int32_t *retStamp[2] = {nullptr, nullptr}, *fullSplit = nullptr;
   int32_t denseAlpha = 10;  // dense (pull) round when out-edges * alpha > E
   int32_t *fvid[2] = {nullptr, nullptr}, *fpre[2] = {nullptr, nullptr};
   int32_t *fbeg[2] = {nullptr, nullptr};
@@ -169,7 +169,7 @@ namespace {
 
 void free_graph(gas_core *c) {
   void *ptrs[] = {c->inOff, c->inSrc, c->outOff, c->outDst, c->ed, c->vd, c->vnew, c->vsaved,
-                  c->valt, c->retStamp, c->fullSplit,
+                  c->valt, c->retStamp[0], c->retStamp[1], c->fullSplit,
                   c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
@@ -178,7 +178,7 @@ void free_graph(gas_core *c) {
     if (p) cudaFree(p);
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
-  c->retStamp = c->fullSplit = nullptr;
+  c->retStamp[0] = c->retStamp[1] = c->fullSplit = nullptr;
   for (int k = 0; k < 2; ++k) {
     c->fvid[k] = c->fpre[k] = c->fbeg[k] = c->fsplit[k] = nullptr;
     c->svid[k] = c->spre[k] = c->sbeg[k] = c->ssplit[k] = nullptr;
@@ -368,7 +368,8 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(cudaMalloc(&c->vd, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->vnew, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->valt, (size_t)vertexBytes * std::max(nV, 1)));
-  A(dalloc(&c->retStamp, (size_t)nV));
+  A(dalloc(&c->retStamp[0], (size_t)nV));
+  A(dalloc(&c->retStamp[1], (size_t)nV));
   A(dalloc(&c->fullSplit, (size_t)c->maxGatherTiles));
   for (int k = 0; k < 2; ++k) {
     A(dalloc(&c->fvid[k], (size_t)nV));
@@ -412,7 +413,8 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
                       c->stream));
   }
   A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
-  A(cudaMemsetAsync(c->retStamp, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
+  for (int k = 0; k < 2; ++k)
+    A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
   if (nV > 0) {
     const int nsplit = (int)(((long long)nV + nE + GAS_GATHER_TILE - 1) / GAS_GATHER_TILE) + 1;
     gas::detail::range_split_kernel<<<(nsplit + 127) / 128, 128, 0, c->stream>>>(
@@ -760,7 +762,8 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   }
   if (c->stamp > 0x40000000) {
     A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
-    A(cudaMemsetAsync(c->retStamp, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
+    for (int k = 0; k < 2; ++k)
+      A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
     c->stamp = 0;
   }
   A(cudaMemsetAsync(&c->ctl->dense[0][0], 0, sizeof(c->ctl->dense), c->stream));
@@ -811,7 +814,8 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.barrier = &c->ctl->bar[0];
   ra.roundsOut = &c->ctl->rounds;
   ra.vertexAlt = c->valt;
-  ra.retStamp = c->retStamp;
+  ra.retStamp[0] = c->retStamp[0];
+  ra.retStamp[1] = c->retStamp[1];
   ra.fullSplit = c->fullSplit;
   ra.denseCnt = &c->ctl->dense[0][0];
   ra.denseAlpha = c->denseAlpha;
