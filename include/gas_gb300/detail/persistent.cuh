@@ -123,9 +123,11 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
       *ra.frontL[cur ^ 1].maxDeg = 0u;
       *ra.scatL[sidx ^ 1].count = 0ull;  // appended by the next round's gather
       *ra.scatL[sidx ^ 1].maxDeg = 0u;
-      unsigned long long *nextCnt = ra.denseCnt + 2 * ((r + 1) % 3);
-      nextCnt[0] = 0ull;
-      nextCnt[1] = 0ull;
+      if (ra.denseCnt) {  // absent when dense rounds are disabled
+        unsigned long long *nextCnt = ra.denseCnt + 2 * ((r + 1) % 3);
+        nextCnt[0] = 0ull;
+        nextCnt[1] = 0ull;
+      }
     }
     unsigned long long statA, statR;
     bool denseNext;
