@@ -13,12 +13,22 @@
 // previous round's set while it records its own.
 //
 // which is exactly the set the reference's scatterActivate builds, so the
-// active sets and round counts are unchanged.  The pass walks the whole CSC
-// in merge-path tiles whose splits are fixed per graph (so FP reductions
-// are associated the same way every run), gathers speculatively, applies
-// to the active vertices and writes every vertex's data to the other
-// buffer of a ping-pong pair: no commit, no scatter traversal, no frontier
-// list, one grid barrier per round.
+// active sets and round counts are unchanged.  The pass gathers
+// speculatively, applies to the active vertices and writes every vertex's
+// data to the other buffer of a ping-pong pair: no commit, no scatter
+// traversal, no frontier list, one grid barrier per round.
+//
+// Load balance is fixed per graph by in-degree bins, each vertex owned by
+// one warp work unit, with no block barriers and no waits:
+//   in-degree 0..8      one thread, edges folded left to right from
+//                       gatherZero (the order of refgas.h:147-158);
+//   in-degree 9..64     8 lanes, ordered shuffle tree;
+//   in-degree 65..1024  one warp, ordered shuffle tree;
+//   in-degree > 1024    1024-edge chunks, one warp each; the warp that
+//                       finishes a vertex's last chunk (arrival counter)
+//                       combines the partials in chunk order.
+// Each vertex's reduction order depends only on its degree, so results are
+// identical run to run.
 #pragma once
 
 #include "gather.cuh"
@@ -33,249 +43,255 @@ struct DenseCtx {
   const int32_t *inSources;
   const int32_t *outOffsets;
   const void *edgeData;
-  const int32_t *split;  // gather-tile splits of [0, nVertices)
   const void *vdCur;
   void *vdNext;
   const int32_t *prevRet;  // stamps written by the previous round (read only here)
   int32_t *curRet;         // stamps of this round (the other array of the pair)
   int32_t prevStamp;       // stamp of the previous round's apply-returned-true set
   int32_t curStamp;
-  int32_t allActive;     // every vertex active (setActive(0, V))
+  int32_t allActive;       // every vertex active (setActive(0, V))
   int32_t haveGather;
-  void *carryVal;
-  unsigned *carryFlag;
-  unsigned epoch;
-  unsigned *errWord;
   int32_t iteration;
   unsigned long long *cnt;  // [2]: (active << 32 | in-edges), (ret << 32 | out-edges)
+  // degree bins, fixed per graph
+  const int32_t *binMid;
+  const int32_t *binSmall;
+  const int32_t *binTiny;
+  int32_t nMid, nSmall, nTiny;
+  const int32_t *chunkVertex;
+  const int32_t *chunkBegin;
+  const int32_t *chunkFirst;
+  const int32_t *chunkCount;
+  const int32_t *chunkSlot;
+  int32_t nChunks;
+  unsigned *chunkArrive;
+  void *chunkVal;
+  unsigned *chunkFlags;
+};
+
+constexpr int kChunkEdges = 1024;  // edges per chunk of a large vertex
+constexpr int kSmallLanes = 8;     // lanes per vertex of in-degree 9..64
+
+// Per-lane accumulators of one edge stream: reduction, "has an edge",
+// "some edge activates the vertex".
+template <typename GR>
+struct EdgeAcc {
+  unsigned has;
+  unsigned act;
+  GR val;
 };
 
 template <class P>
-struct DenseSmem {
-  int32_t end[kGTILE];
-  SegScanSmem<typename P::GatherResult, kGNT> seg;
-  int32_t headPre;
-  unsigned lookHas;
-  unsigned lookAct;
-  typename P::GatherResult lookVal;
-};
-
-template <class P>
-__device__ void dense_tile(const DenseCtx &a, int t, DenseSmem<P> &sm) {
+__device__ __forceinline__ void edge_step(const DenseCtx &a, int v, int e,
+                                          EdgeAcc<typename P::GatherResult> &x) {
   typedef typename P::VertexData VD;
-  typedef typename P::GatherResult GR;
-  const int tid = threadIdx.x;
-  const long long total = (long long)a.nVertices + a.nEdges;
-  const int d0 = t * kGTILE;
-  const int d1 = (int)min((long long)d0 + kGTILE, total);
-  const int i0 = a.split[t];
-  const int i1 = (d1 == total) ? a.nVertices : a.split[t + 1];
-  const int j0 = d0 - i0, j1 = d1 - i1;
-  const int nb = i1 - i0, na = j1 - j0;
   const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
-  for (int m = tid; m < nb; m += kGNT) sm.end[m] = a.inOffsets[i0 + m + 1] - j0;
-  if (tid == 0) sm.headPre = i0 < a.nVertices ? a.inOffsets[i0] : a.nEdges;
-  __syncthreads();
-
-  const int tileItems = d1 - d0;
-  const int dl = tid * kGVT;
-  int bi = 0;
-  if (dl < tileItems) {
-    int lo = max(0, dl - na), hi = min(dl, nb);
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (sm.end[mid - 1] <= dl - mid)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    bi = lo;
+  const int src = __ldg(a.inSources + e);
+  x.act |= (a.allActive || a.prevRet[src] == a.prevStamp) ? 1u : 0u;
+  if (a.haveGather) {
+    const typename P::GatherResult m = P::gatherMap(vd + v, vd + src, edge_ptr<P>(a.edgeData, e));
+    x.val = x.has ? P::gatherReduce(x.val, m) : m;
   }
-  int aj = dl - bi;
-  int kind[kGVT], vloc[kGVT], phys[kGVT];
+  x.has = 1u;
+}
+
+// Ordered tree combine of lane accumulators within aligned groups of
+// `width` lanes; lane 0 of each group ends with the group's combination.
+template <class P, int W>
+__device__ __forceinline__ void group_reduce(EdgeAcc<typename P::GatherResult> &x) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int v = 0; v < kGVT; ++v) {
-    kind[v] = 0;
-    vloc[v] = 0;
-    phys[v] = 0;
-    if (dl + v < tileItems) {
-      if (bi < nb && (aj >= na || sm.end[bi] <= aj)) {
-        kind[v] = 2;
-        vloc[v] = bi;
-        ++bi;
-      } else {
-        kind[v] = 1;
-        vloc[v] = bi;
-        phys[v] = j0 + aj;
-        ++aj;
+  for (int d = 1; d < W; d <<= 1) {
+    const unsigned oh = __shfl_down_sync(kFullMask, x.has, d, W);
+    const unsigned oa = __shfl_down_sync(kFullMask, x.act, d, W);
+    const typename P::GatherResult ov = shfl_down_any_w(x.val, d, W);
+    if ((lane & (2 * d - 1)) == 0) {
+      x.act |= oa;
+      if (oh) {
+        x.val = x.has ? P::gatherReduce(x.val, ov) : ov;
+        x.has = 1u;
       }
     }
   }
-  int src[kGVT];
-#pragma unroll
-  for (int v = 0; v < kGVT; ++v) src[v] = (kind[v] == 1) ? __ldg(a.inSources + phys[v]) : 0;
-  unsigned eact[kGVT];
-#pragma unroll
-  for (int v = 0; v < kGVT; ++v)
-    eact[v] = (kind[v] == 1) && (a.allActive || a.prevRet[src[v]] == a.prevStamp) ? 1u : 0u;
+}
+
+struct DenseCounts {
+  unsigned active, inEdges, ret, outEdges;
+};
+
+// Final gather result of a vertex from its combined (tree-ordered) state.
+template <class P>
+__device__ __forceinline__ typename P::GatherResult
+combined_result(const DenseCtx &a, const EdgeAcc<typename P::GatherResult> &x) {
+  const typename P::GatherResult gz = P::gatherZero;
+  return (a.haveGather && x.has) ? P::gatherReduce(gz, x.val) : gz;
+}
+
+// apply() for vertex v; every vertex is written to vdNext.
+template <class P>
+__device__ __forceinline__ void dense_finish(const DenseCtx &a, int v, unsigned act,
+                                             const typename P::GatherResult &g, int inDeg,
+                                             DenseCounts &c) {
+  typedef typename P::VertexData VD;
+  const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
+  VD tmp = vd[v];
+  if (a.allActive || act) {
+    const bool r = do_apply<P>(&tmp, g, a.iteration);
+    ++c.active;
+    c.inEdges += (unsigned)inDeg;
+    if (r) {
+      a.curRet[v] = a.curStamp;
+      ++c.ret;
+      c.outEdges += (unsigned)(a.outOffsets[v + 1] - a.outOffsets[v]);
+    }
+  }
+  reinterpret_cast<VD *>(a.vdNext)[v] = tmp;
+}
+
+// Warp work units of one dense pass: [large-vertex chunks | one vertex per
+// warp | 8-lane groups | one vertex per thread].
+__device__ __forceinline__ long long dense_units(const DenseCtx &a) {
+  return (long long)a.nChunks + a.nMid + (a.nSmall + 3) / 4 + (a.nTiny + 31) / 32;
+}
+
+template <class P>
+__device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) {
+  typedef typename P::GatherResult GR;
+  const int lane = threadIdx.x & 31;
   const GR gz = P::gatherZero;
-  GR val[kGVT];
-#pragma unroll
-  for (int v = 0; v < kGVT; ++v) {
-    val[v] = gz;
-    if (kind[v] == 1 && a.haveGather)
-      val[v] = P::gatherMap(vd + (i0 + vloc[v]), vd + src[v], edge_ptr<P>(a.edgeData, phys[v]));
-  }
-
-  // ---- fold: per segment (vertex) the reduction and the activation OR
-  unsigned has = 0u, act = 0u;
-  GR acc = gz;
-  bool segHas[kGVT];
-  unsigned segAct[kGVT];
-  GR segVal[kGVT];
-  unsigned anyEnd = 0u;
-#pragma unroll
-  for (int v = 0; v < kGVT; ++v) {
-    segHas[v] = false;
-    segAct[v] = 0u;
-    if (kind[v] == 1) {
-      acc = has ? P::gatherReduce(acc, val[v]) : val[v];
-      has = 1u;
-      act |= eact[v];
-    } else if (kind[v] == 2) {
-      segHas[v] = has != 0u;
-      segAct[v] = act;
-      segVal[v] = acc;
-      has = 0u;
-      act = 0u;
-      anyEnd = 1u;
+  EdgeAcc<GR> x;
+  x.has = 0u;
+  x.act = 0u;
+  x.val = gz;
+  if (u < a.nChunks) {
+    // ---- one chunk of a large vertex; the last chunk to finish combines
+    const int ch = (int)u;
+    const int v = a.chunkVertex[ch];
+    const int beg = a.chunkBegin[ch];
+    const int end = min(beg + kChunkEdges, a.inOffsets[v + 1]);
+    for (int e = beg + lane; e < end; e += 32) edge_step<P>(a, v, e, x);
+    group_reduce<P, 32>(x);
+    unsigned last = 0u;
+    if (lane == 0) {
+      if (x.has) reinterpret_cast<GR *>(a.chunkVal)[ch] = x.val;
+      a.chunkFlags[ch] = x.has | (x.act << 1);
+      __threadfence();
+      const unsigned prev = atomicAdd(a.chunkArrive + a.chunkSlot[ch], 1u);
+      last = (prev + 1 == (unsigned)a.chunkCount[ch]) ? 1u : 0u;
+      if (last) __threadfence();
     }
-  }
-  SegVal<GR> mine;
-  mine.end = anyEnd;
-  mine.has = has;
-  mine.act = act;
-  mine.val = acc;
-  SegVal<GR> excl, tot;
-  block_seg_scan<P, GR, kGNT>(mine, excl, tot, sm.seg);
-
-  if (tid == kGNT - 1 && tot.has) {
-    reinterpret_cast<GR *>(a.carryVal)[t] = tot.val;
-    __threadfence();
-    publish_flag(a.carryFlag + t, a.epoch, tot.act);
-  }
-  const bool headSplit = nb > 0 && sm.headPre < j0;
-  if (tid < 32) {
-    if (headSplit) {
-      const int ts = (int)(((long long)sm.headPre + i0) / kGTILE);
-      unsigned lh = 0u, la = 0u;
-      GR lv = gz;
-      for (int c0 = ts; c0 < t; c0 += 32) {
-        const int ti = c0 + tid;
-        const int cnt = min(32, t - c0);
-        unsigned h = 0u, xa = 0u;
-        GR x = gz;
-        if (ti < t) {
-          unsigned fa;
-          if (wait_epoch(a.carryFlag + ti, a.epoch, a.errWord, &fa)) {
-            x = load_cg(reinterpret_cast<const GR *>(a.carryVal) + ti);
-            h = 1u;
-            xa = fa;
-          }
-        }
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          unsigned oh = __shfl_down_sync(kFullMask, h, d);
-          unsigned oa = __shfl_down_sync(kFullMask, xa, d);
-          GR ox = shfl_down_any(x, d);
-          if ((tid & (2 * d - 1)) == 0 && tid + d < cnt) {
-            xa |= oa;
-            if (oh) {
-              x = h ? P::gatherReduce(x, ox) : ox;
-              h = 1u;
-            }
-          }
-        }
-        if (tid == 0) {
-          la |= xa;
-          if (h) {
-            lv = lh ? P::gatherReduce(lv, x) : x;
-            lh = 1u;
-          }
+    last = __shfl_sync(kFullMask, last, 0);
+    if (!last) return;
+    const int first = a.chunkFirst[ch], count = a.chunkCount[ch];
+    EdgeAcc<GR> tot;
+    tot.has = 0u;
+    tot.act = 0u;
+    tot.val = gz;
+    for (int c0 = 0; c0 < count; c0 += 32) {
+      EdgeAcc<GR> y;
+      y.has = 0u;
+      y.act = 0u;
+      y.val = gz;
+      if (c0 + lane < count) {
+        const unsigned f = __ldcg(a.chunkFlags + first + c0 + lane);
+        y.has = f & 1u;
+        y.act = (f >> 1) & 1u;
+        if (y.has) y.val = load_cg(reinterpret_cast<const GR *>(a.chunkVal) + first + c0 + lane);
+      }
+      group_reduce<P, 32>(y);
+      if (lane == 0) {
+        tot.act |= y.act;
+        if (y.has) {
+          tot.val = tot.has ? P::gatherReduce(tot.val, y.val) : y.val;
+          tot.has = 1u;
         }
       }
-      if (tid == 0) {
-        sm.lookHas = lh;
-        sm.lookAct = la;
-        sm.lookVal = lv;
-      }
-    } else if (tid == 0) {
-      sm.lookHas = 0u;
-      sm.lookAct = 0u;
     }
-  }
-  __syncthreads();
-
-  unsigned preHas = 0u, preAct = 0u;
-  GR preVal = gz;
-  if (!excl.end && headSplit) {
-    preAct = sm.lookAct;
-    if (sm.lookHas) {
-      preVal = sm.lookVal;
-      preHas = 1u;
+    if (lane == 0) {
+      a.chunkArrive[a.chunkSlot[ch]] = 0u;  // ready for the next dense round
+      dense_finish<P>(a, v, tot.act, combined_result<P>(a, tot), a.inOffsets[v + 1] - a.inOffsets[v], c);
     }
+    return;
   }
-  preAct |= excl.act;
-  if (excl.has) {
-    preVal = preHas ? P::gatherReduce(preVal, excl.val) : excl.val;
-    preHas = 1u;
+  u -= a.nChunks;
+  if (u < a.nMid) {
+    // ---- one vertex per warp (in-degree 65..1024)
+    const int v = a.binMid[u];
+    const int beg = a.inOffsets[v], end = a.inOffsets[v + 1];
+    for (int e = beg + lane; e < end; e += 32) edge_step<P>(a, v, e, x);
+    group_reduce<P, 32>(x);
+    if (lane == 0) dense_finish<P>(a, v, x.act, combined_result<P>(a, x), end - beg, c);
+    return;
   }
-  bool firstDone = false;
+  u -= a.nMid;
+  const long long smallGroups = (a.nSmall + 3) / 4;
+  if (u < smallGroups) {
+    // ---- one vertex per 8 lanes (in-degree 9..64)
+    const long long idx = u * 4 + lane / kSmallLanes;
+    const int sl = lane % kSmallLanes;
+    int v = -1, beg = 0, end = 0;
+    if (idx < a.nSmall) {
+      v = a.binSmall[idx];
+      beg = a.inOffsets[v];
+      end = a.inOffsets[v + 1];
+    }
 #pragma unroll
-  for (int v = 0; v < kGVT; ++v) {
-    if (kind[v] == 2 && !firstDone) {
-      firstDone = true;
-      segAct[v] |= preAct;
-      if (preHas) {
-        segVal[v] = segHas[v] ? P::gatherReduce(preVal, segVal[v]) : preVal;
-        segHas[v] = true;
-      }
+    for (int k = 0; k < 64 / kSmallLanes; ++k) {
+      const int e = beg + sl + k * kSmallLanes;
+      if (e < end) edge_step<P>(a, v, e, x);
     }
+    group_reduce<P, kSmallLanes>(x);
+    if (sl == 0 && v >= 0) dense_finish<P>(a, v, x.act, combined_result<P>(a, x), end - beg, c);
+    return;
   }
-
-  // ---- apply to active vertices; every vertex is written to vdNext
-  VD *vnext = reinterpret_cast<VD *>(a.vdNext);
-  unsigned nA = 0, nEin = 0, nR = 0, nEout = 0;
+  u -= smallGroups;
+  {
+    // ---- one vertex per thread (in-degree 0..8), folded left to right
+    // from gatherZero exactly as refgas.h:147-158
+    const long long idx = u * 32 + lane;
+    if (idx >= a.nTiny) return;
+    const int v = a.binTiny[idx];
+    const int beg = a.inOffsets[v], end = a.inOffsets[v + 1];
+    typedef typename P::VertexData VD;
+    const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
+    int src[GAS_TPV_MAX_DEGREE];
 #pragma unroll
-  for (int v = 0; v < kGVT; ++v) {
-    if (kind[v] == 2) {
-      const int m = vloc[v];
-      const int vx = i0 + m;
-      VD tmp = vd[vx];
-      if (a.allActive || segAct[v]) {  // with every vertex active, in-degree 0 too
-        GR g = gz;
-        if (a.haveGather && segHas[v]) g = P::gatherReduce(gz, segVal[v]);
-        const bool r = do_apply<P>(&tmp, g, a.iteration);
-        const int start = (m == 0) ? sm.headPre - j0 : sm.end[m - 1];
-        ++nA;
-        nEin += (unsigned)(sm.end[m] - start);
-        if (r) {
-          a.curRet[vx] = a.curStamp;
-          ++nR;
-          nEout += (unsigned)(a.outOffsets[vx + 1] - a.outOffsets[vx]);
-        }
+    for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k)
+      src[k] = beg + k < end ? __ldg(a.inSources + beg + k) : 0;
+    GR g = gz;
+    unsigned act = 0u;
+#pragma unroll
+    for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k)
+      if (beg + k < end) {
+        act |= (a.allActive || a.prevRet[src[k]] == a.prevStamp) ? 1u : 0u;
+        if (a.haveGather)
+          g = P::gatherReduce(g, P::gatherMap(vd + v, vd + src[k], edge_ptr<P>(a.edgeData, beg + k)));
       }
-      vnext[vx] = tmp;
-    }
+    dense_finish<P>(a, v, act, g, end - beg, c);
   }
-  const unsigned wA = __reduce_add_sync(kFullMask, nA);
-  const unsigned wEin = __reduce_add_sync(kFullMask, nEin);
-  const unsigned wR = __reduce_add_sync(kFullMask, nR);
-  const unsigned wEout = __reduce_add_sync(kFullMask, nEout);
-  if ((tid & 31) == 0) {
+}
+
+// Flushes a warp's counts (one pair of atomics per warp and pass).
+__device__ __forceinline__ void dense_flush(const DenseCtx &a, const DenseCounts &c) {
+  const unsigned wA = __reduce_add_sync(kFullMask, c.active);
+  const unsigned wEin = __reduce_add_sync(kFullMask, c.inEdges);
+  const unsigned wR = __reduce_add_sync(kFullMask, c.ret);
+  const unsigned wEout = __reduce_add_sync(kFullMask, c.outEdges);
+  if ((threadIdx.x & 31) == 0) {
     if (wA) atomicAdd(a.cnt, ((unsigned long long)wA << 32) | wEin);
     if (wR) atomicAdd(a.cnt + 1, ((unsigned long long)wR << 32) | wEout);
   }
+}
+
+// One dense pass over every vertex, warp units assigned statically.
+template <class P>
+__device__ void dense_pass(const DenseCtx &a) {
+  DenseCounts c = {0u, 0u, 0u, 0u};
+  const long long units = dense_units(a);
+  const long long warps = (long long)gridDim.x * (blockDim.x / 32);
+  for (long long u = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; u < units; u += warps)
+    dense_warp_unit<P>(a, u, c);
+  dense_flush(a, c);
 }
 
 // Dense -> list transition: the vertices stamped in this round become the

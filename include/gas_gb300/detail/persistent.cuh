@@ -10,7 +10,7 @@
 //   -> grid barrier -> swap frontier, next round
 //
 // Rounds whose predecessor activated many out-edges run dense (pull, see
-// dense.cuh): one pass and one barrier.  Transitions build the other
+// dense.cuh): one pass of degree-binned warp units and one barrier.  Transitions build the other
 // representation: list -> dense stamps the scatter list, dense -> list
 // compacts the stamped vertices into a scatter list and pushes it.
 //
@@ -69,7 +69,6 @@ template <class P>
 union PersistentSmem {
   GatherSmem<P> g;
   ScatterSmem s;
-  DenseSmem<P> d;
 };
 
 template <class P>
@@ -101,11 +100,22 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
   dc.inSources = a.inSources;
   dc.outOffsets = a.outOffsets;
   dc.edgeData = a.edgeData;
-  dc.split = ra.fullSplit;
+  dc.binMid = ra.binMid;
+  dc.binSmall = ra.binSmall;
+  dc.binTiny = ra.binTiny;
+  dc.nMid = ra.nMid;
+  dc.nSmall = ra.nSmall;
+  dc.nTiny = ra.nTiny;
+  dc.chunkVertex = ra.chunkVertex;
+  dc.chunkBegin = ra.chunkBegin;
+  dc.chunkFirst = ra.chunkFirst;
+  dc.chunkCount = ra.chunkCount;
+  dc.chunkSlot = ra.chunkSlot;
+  dc.nChunks = ra.nChunks;
+  dc.chunkArrive = ra.chunkArrive;
+  dc.chunkVal = ra.chunkVal;
+  dc.chunkFlags = ra.chunkFlags;
   dc.haveGather = a.haveGather;
-  dc.carryVal = a.carryVal;
-  dc.carryFlag = a.carryFlag;
-  dc.errWord = a.errWord;
   void *vdBuf[2] = {a.vertexData, ra.vertexAlt};
   const long long E = a.nEdges;
 
@@ -188,14 +198,9 @@ __global__ void __launch_bounds__(kGNT) run_persistent_kernel(const gas_run_args
       dc.prevStamp = stamp - 1;
       dc.curStamp = stamp;
       dc.allActive = allActive ? 1 : 0;
-      dc.epoch = epoch;
       dc.iteration = ra.g.iteration + r;
       dc.cnt = ra.denseCnt + 2 * (r % 3);
-      const int ntD = (int)(((long long)a.nVertices + a.nEdges + kGTILE - 1) / kGTILE);
-      for (int t = blockIdx.x; t < ntD; t += gridDim.x) {
-        dense_tile<P>(dc, t, sm.d);
-        __syncthreads();
-      }
+      dense_pass<P>(dc);
       if (!grid_barrier(ra.barrier, a.errWord)) break;
       statA = dc.cnt[0];
       statR = dc.cnt[1];

@@ -46,6 +46,18 @@ __device__ __forceinline__ T shfl_down_any(const T &v, int delta) {
 }
 
 template <typename T>
+__device__ __forceinline__ T shfl_down_any_w(const T &v, int delta, int width) {
+  constexpr int W = (int)((sizeof(T) + 3) / 4);
+  uint32_t w[W];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int k = 0; k < W; ++k) w[k] = __shfl_down_sync(kFullMask, w[k], delta, width);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <typename T>
 __device__ __forceinline__ T shfl_any(const T &v, int lane) {
   constexpr int W = (int)((sizeof(T) + 3) / 4);
   uint32_t w[W];

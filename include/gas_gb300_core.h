@@ -121,11 +121,26 @@ typedef struct {
   void *vertexAlt;            /* second vertex-data buffer (ping-pong)      */
   int32_t *retStamp[2];       /* [V] each: stamp of the round whose apply returned
                                  true; round r writes [r & 1] and reads [(r-1) & 1] */
-  const int32_t *fullSplit;   /* gather-tile splits of [0, V)               */
   unsigned long long *denseCnt; /* [3][2] per-round counters                */
   int32_t denseAlpha;         /* next round dense when out-edges*alpha > E; 0 = never */
   int32_t allActive;          /* round 0 is every vertex (setActive(0, V)) */
   int32_t *vcurOut;           /* 1 when the final vertex data is in vertexAlt */
+  /* degree bins of the dense pass (fixed per graph): warp work units are
+   * [large-vertex chunks | warp-per-vertex | 8-lane groups | thread-per-vertex] */
+  const int32_t *binMid;      /* in-degree 65..1024: one warp each          */
+  const int32_t *binSmall;    /* in-degree 9..64: 8 lanes each              */
+  const int32_t *binTiny;     /* in-degree 0..8: one thread each            */
+  int32_t nMid, nSmall, nTiny;
+  const int32_t *chunkVertex; /* in-degree > 1024: 1024-edge chunks          */
+  const int32_t *chunkBegin;  /* first CSC position of each chunk            */
+  const int32_t *chunkFirst;  /* index of the vertex's first chunk, per chunk */
+  const int32_t *chunkCount;  /* chunks of the vertex, per chunk             */
+  const int32_t *chunkSlot;   /* arrival-counter slot of the vertex, per chunk */
+  int32_t nChunks;
+  int32_t nChunkVertices;
+  unsigned *chunkArrive;      /* [2][nChunkVertices] arrival counters        */
+  void *chunkVal;             /* [nChunks] GatherResult partials             */
+  unsigned *chunkFlags;       /* [nChunks] has | act << 1                    */
 } gas_run_args;
 
 typedef struct gas_core_s gas_core;

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "gas_gb300_core.h"
+#include "gas_gb300/detail/dense.cuh"
 #include "gas_gb300/detail/scatter.cuh"
 #include "gas_internal.h"
 
@@ -125,7 +126,15 @@ struct gas_core_s {
   int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
   void *ed = nullptr;
   void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr, *valt = nullptr;
-  int32_t *retStamp[2] = {nullptr, nullptr}, *fullSplit = nullptr;
+  int32_t *retStamp[2] = {nullptr, nullptr};
+  // degree bins of the dense pass (see dense.cuh)
+  int32_t *binMid = nullptr, *binSmall = nullptr, *binTiny = nullptr;
+  int32_t nMid = 0, nSmall = 0, nTiny = 0;
+  int32_t *chunkVertex = nullptr, *chunkBegin = nullptr, *chunkFirst = nullptr;
+  int32_t *chunkCount = nullptr, *chunkSlot = nullptr;
+  int32_t nChunks = 0, nChunkVertices = 0;
+  unsigned *chunkArrive = nullptr, *chunkFlags = nullptr;
+  void *chunkVal = nullptr;
   int32_t denseAlpha = 10;  // dense (pull) round when out-edges * alpha > E
   int32_t *fvid[2] = {nullptr, nullptr}, *fpre[2] = {nullptr, nullptr};
   int32_t *fbeg[2] = {nullptr, nullptr};
@@ -169,7 +178,9 @@ namespace {
 
 void free_graph(gas_core *c) {
   void *ptrs[] = {c->inOff, c->inSrc, c->outOff, c->outDst, c->ed, c->vd, c->vnew, c->vsaved,
-                  c->valt, c->retStamp[0], c->retStamp[1], c->fullSplit,
+                  c->valt, c->retStamp[0], c->retStamp[1], c->binMid, c->binSmall,
+                  c->binTiny, c->chunkVertex, c->chunkBegin, c->chunkFirst, c->chunkCount,
+                  c->chunkSlot, c->chunkArrive, c->chunkFlags, c->chunkVal,
                   c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
@@ -178,7 +189,12 @@ void free_graph(gas_core *c) {
     if (p) cudaFree(p);
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
-  c->retStamp[0] = c->retStamp[1] = c->fullSplit = nullptr;
+  c->retStamp[0] = c->retStamp[1] = nullptr;
+  c->binMid = c->binSmall = c->binTiny = nullptr;
+  c->chunkVertex = c->chunkBegin = c->chunkFirst = c->chunkCount = c->chunkSlot = nullptr;
+  c->chunkArrive = c->chunkFlags = nullptr;
+  c->chunkVal = nullptr;
+  c->nMid = c->nSmall = c->nTiny = c->nChunks = c->nChunkVertices = 0;
   for (int k = 0; k < 2; ++k) {
     c->fvid[k] = c->fpre[k] = c->fbeg[k] = c->fsplit[k] = nullptr;
     c->svid[k] = c->spre[k] = c->sbeg[k] = c->ssplit[k] = nullptr;
@@ -370,7 +386,44 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(cudaMalloc(&c->valt, (size_t)vertexBytes * std::max(nV, 1)));
   A(dalloc(&c->retStamp[0], (size_t)nV));
   A(dalloc(&c->retStamp[1], (size_t)nV));
-  A(dalloc(&c->fullSplit, (size_t)c->maxGatherTiles));
+  // in-degree bins of the dense pass
+  std::vector<int32_t> bMid, bSmall, bTiny, chV, chB, chF, chC, chS;
+  for (int32_t v = 0; v < nV; ++v) {
+    const int32_t deg = c->hInOff[(size_t)v + 1] - c->hInOff[v];
+    if (deg <= GAS_TPV_MAX_DEGREE) {
+      bTiny.push_back(v);
+    } else if (deg <= 64) {
+      bSmall.push_back(v);
+    } else if (deg <= gas::detail::kChunkEdges) {
+      bMid.push_back(v);
+    } else {
+      const int32_t nch = (deg + gas::detail::kChunkEdges - 1) / gas::detail::kChunkEdges;
+      const int32_t first = (int32_t)chV.size(), slot = (int32_t)(chS.empty() ? 0 : chS.back() + 1);
+      for (int32_t k = 0; k < nch; ++k) {
+        chV.push_back(v);
+        chB.push_back(c->hInOff[v] + k * gas::detail::kChunkEdges);
+        chF.push_back(first);
+        chC.push_back(nch);
+        chS.push_back(slot);
+      }
+    }
+  }
+  c->nMid = (int32_t)bMid.size();
+  c->nSmall = (int32_t)bSmall.size();
+  c->nTiny = (int32_t)bTiny.size();
+  c->nChunks = (int32_t)chV.size();
+  c->nChunkVertices = chS.empty() ? 0 : chS.back() + 1;
+  A(dalloc(&c->binMid, bMid.size()));
+  A(dalloc(&c->binSmall, bSmall.size()));
+  A(dalloc(&c->binTiny, bTiny.size()));
+  A(dalloc(&c->chunkVertex, chV.size()));
+  A(dalloc(&c->chunkBegin, chB.size()));
+  A(dalloc(&c->chunkFirst, chF.size()));
+  A(dalloc(&c->chunkCount, chC.size()));
+  A(dalloc(&c->chunkSlot, chS.size()));
+  A(dalloc(&c->chunkArrive, (size_t)c->nChunkVertices));
+  A(dalloc(&c->chunkFlags, chV.size()));
+  A(cudaMalloc(&c->chunkVal, (size_t)((gatherBytes + 15) / 16 * 16) * std::max<size_t>(chV.size(), 1)));
   for (int k = 0; k < 2; ++k) {
     A(dalloc(&c->fvid[k], (size_t)nV));
     A(dalloc(&c->fpre[k], (size_t)nV));
@@ -415,12 +468,20 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
   for (int k = 0; k < 2; ++k)
     A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
-  if (nV > 0) {
-    const int nsplit = (int)(((long long)nV + nE + GAS_GATHER_TILE - 1) / GAS_GATHER_TILE) + 1;
-    gas::detail::range_split_kernel<<<(nsplit + 127) / 128, 128, 0, c->stream>>>(
-        c->inOff, 0, nV, nE, c->fullSplit, nsplit);
-    A(cudaGetLastError());
-  }
+  auto up = [&](int32_t *dst, const std::vector<int32_t> &src) {
+    if (!src.empty())
+      A(cudaMemcpyAsync(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice,
+                        c->stream));
+  };
+  up(c->binMid, bMid);
+  up(c->binSmall, bSmall);
+  up(c->binTiny, bTiny);
+  up(c->chunkVertex, chV);
+  up(c->chunkBegin, chB);
+  up(c->chunkFirst, chF);
+  up(c->chunkCount, chC);
+  up(c->chunkSlot, chS);
+  A(cudaMemsetAsync(c->chunkArrive, 0, sizeof(unsigned) * std::max(c->nChunkVertices, 1), c->stream));
   A(cudaMemsetAsync(c->carryFlag, 0, sizeof(unsigned) * c->maxGatherTiles, c->stream));
   A(cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream));
   A(cudaMemsetAsync(c->vd, 0, (size_t)vertexBytes * std::max(nV, 1), c->stream));
@@ -767,6 +828,7 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
     c->stamp = 0;
   }
   A(cudaMemsetAsync(&c->ctl->dense[0][0], 0, sizeof(c->ctl->dense), c->stream));
+  A(cudaMemsetAsync(c->chunkArrive, 0, sizeof(unsigned) * std::max(c->nChunkVertices, 1), c->stream));
   A(cudaMemsetAsync(&c->ctl->s[0], 0, sizeof(c->ctl->s), c->stream));
   A(cudaMemsetAsync(&c->ctl->f[c->cur ^ 1], 0, sizeof(ListCtl), c->stream));
   A(cudaMemsetAsync(&c->ctl->bar[0], 0, sizeof(c->ctl->bar) + sizeof(int32_t), c->stream));
@@ -816,7 +878,22 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.vertexAlt = c->valt;
   ra.retStamp[0] = c->retStamp[0];
   ra.retStamp[1] = c->retStamp[1];
-  ra.fullSplit = c->fullSplit;
+  ra.binMid = c->binMid;
+  ra.binSmall = c->binSmall;
+  ra.binTiny = c->binTiny;
+  ra.nMid = c->nMid;
+  ra.nSmall = c->nSmall;
+  ra.nTiny = c->nTiny;
+  ra.chunkVertex = c->chunkVertex;
+  ra.chunkBegin = c->chunkBegin;
+  ra.chunkFirst = c->chunkFirst;
+  ra.chunkCount = c->chunkCount;
+  ra.chunkSlot = c->chunkSlot;
+  ra.nChunks = c->nChunks;
+  ra.nChunkVertices = c->nChunkVertices;
+  ra.chunkArrive = c->chunkArrive;
+  ra.chunkVal = c->chunkVal;
+  ra.chunkFlags = c->chunkFlags;
   ra.denseCnt = &c->ctl->dense[0][0];
   ra.denseAlpha = c->denseAlpha;
   ra.allActive = (c->rangeMode && c->rstart == 0 && c->rcount == c->nV && c->denseAlpha > 0) ? 1 : 0;
