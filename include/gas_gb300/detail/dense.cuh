@@ -115,6 +115,32 @@ __device__ __forceinline__ void group_reduce(EdgeAcc<typename P::GatherResult> &
   }
 }
 
+// Lane-strided walk of the edges [beg, end) of vertex v, four edges per
+// lane in flight: all source ids first, then their stamps and data.
+template <class P>
+__device__ __forceinline__ void strided_edges(const DenseCtx &a, int v, int beg, int end,
+                                              EdgeAcc<typename P::GatherResult> &x) {
+  const int lane = threadIdx.x & 31;
+  for (int e0 = beg + lane; e0 < end; e0 += 4 * 32) {
+    int src[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) src[j] = (e0 + 32 * j < end) ? __ldg(a.inSources + e0 + 32 * j) : -1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (src[j] < 0) continue;
+      typedef typename P::VertexData VD;
+      const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
+      x.act |= (a.allActive || a.prevRet[src[j]] == a.prevStamp) ? 1u : 0u;
+      if (a.haveGather) {
+        const typename P::GatherResult m =
+            P::gatherMap(vd + v, vd + src[j], edge_ptr<P>(a.edgeData, e0 + 32 * j));
+        x.val = x.has ? P::gatherReduce(x.val, m) : m;
+      }
+      x.has = 1u;
+    }
+  }
+}
+
 struct DenseCounts {
   unsigned active, inEdges, ret, outEdges;
 };
@@ -169,7 +195,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     const int v = a.chunkVertex[ch];
     const int beg = a.chunkBegin[ch];
     const int end = min(beg + kChunkEdges, a.inOffsets[v + 1]);
-    for (int e = beg + lane; e < end; e += 32) edge_step<P>(a, v, e, x);
+    strided_edges<P>(a, v, beg, end, x);
     group_reduce<P, 32>(x);
     unsigned last = 0u;
     if (lane == 0) {
@@ -218,7 +244,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     // ---- one vertex per warp (in-degree 65..1024)
     const int v = a.binMid[u];
     const int beg = a.inOffsets[v], end = a.inOffsets[v + 1];
-    for (int e = beg + lane; e < end; e += 32) edge_step<P>(a, v, e, x);
+    strided_edges<P>(a, v, beg, end, x);
     group_reduce<P, 32>(x);
     if (lane == 0) dense_finish<P>(a, v, x.act, combined_result<P>(a, x), end - beg, c);
     return;
