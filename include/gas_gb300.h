@@ -183,6 +183,38 @@ GAS_API gas_status gas_bfs_noalloc(int32_t nVertices, int32_t nEdges, const int3
                                    const int32_t *outDests, int32_t source, int32_t *depth,
                                    void *stream, int32_t *rounds);
 
+/* ---------------- batched multi-source queries --------------------------- */
+/* Many BFS or SSSP queries with their own sources on one resident graph
+ * (no counterpart in the reference, which runs one source per engine).
+ * Each group of up to 256 queries is one persistent launch, captured once
+ * per shape into a CUDA graph and replayed; every query's result equals its
+ * single-source gas_engine_run result bit for bit. */
+typedef struct gas_batch_s gas_batch;
+
+GAS_API gas_status gas_batch_create(int32_t device, void *stream, gas_batch **out);
+GAS_API gas_status gas_batch_destroy(gas_batch *b);
+/* Edge list as gas_engine_set_graph; weights (int32, may be NULL) are the
+ * SSSP edge lengths. */
+GAS_API gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
+                                       const int32_t *srcs, const int32_t *dsts,
+                                       const int32_t *weights);
+/* program = GAS_PROGRAM_BFS or GAS_PROGRAM_SSSP.  results (may be NULL) is a
+ * host array of nQueries * nVertices int32, query-major: BFS depth (-1 =
+ * unreached) or SSSP distance (2147383647 = unreached, sssp.cu:32-33).
+ * *rounds receives the largest round count of the batches. */
+GAS_API gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries,
+                                 const int32_t *sources, int32_t *results, int32_t *rounds);
+/* Work units of at most chunkEdges in-edges, CTAs per SM (0 = as many as
+ * fit), CUDA-graph replay on/off.  Results do not depend on them. */
+GAS_API gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocksPerSM,
+                                        int32_t useGraphs);
+/* Times the candidate configurations on nQueries random sources and keeps
+ * the fastest; reports the chosen chunk size and CTAs per SM. */
+GAS_API gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
+                                      int32_t *chunkEdges, int32_t *blocksPerSM);
+/* Device milliseconds of the most recent gas_batch_run. */
+GAS_API gas_status gas_batch_last_ms(gas_batch *b, float *ms);
+
 /* ---------------- status / diagnostics ---------------------------------- */
 GAS_API const char *gas_status_string(gas_status s);
 GAS_API const char *gas_last_error(void);

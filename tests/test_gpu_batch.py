@@ -1,0 +1,68 @@
+"""Batched multi-source BFS / SSSP: every query equals its single-source
+oracle result bit for bit, across batch sizes, work-unit chunkings (hub
+vertices split over many warps) and with or without CUDA-graph replay."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from vertexapi2_gb300 import GASBatch, graphs
+from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
+
+pytestmark = pytest.mark.gpu
+
+
+def check_queries(port, g, program, sources, got):
+    for q, s in enumerate(sources):
+        if program == PROGRAM_BFS:
+            ref, _ = port.bfs(g.n_vertices, g.srcs, g.dsts, int(s))
+        else:
+            ref, _ = port.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, int(s))
+        assert np.array_equal(got[q], ref), f"query {q} (source {s})"
+
+
+@pytest.mark.parametrize("nq", [1, 7, 40, 256, 300])
+def test_batch_matches_single_source_rmat(gpu, port, nq):
+    g = graphs.rmat(12, 16, seed=41, symmetrize=True, weights=(1, 255))
+    rng = np.random.default_rng(nq)
+    sources = rng.integers(0, g.n_vertices, nq).astype(np.int32)
+    with GASBatch() as b:
+        b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+        for program in (PROGRAM_BFS, PROGRAM_SSSP):
+            got, rounds = b.run(program, sources)
+            assert rounds > 0
+            check_queries(port, g, program, sources[: min(nq, 64)], got)
+
+
+@pytest.mark.parametrize("chunk,graphs_on", [(1, True), (32, False), (2048, True)])
+def test_batch_configs_directed_and_grid(gpu, port, chunk, graphs_on):
+    for g in (graphs.rmat(11, 16, seed=42, weights=(1, 100)),
+              graphs.grid(48, 40, 0.15, seed=43)):
+        rng = np.random.default_rng(chunk)
+        sources = rng.integers(0, g.n_vertices, 33).astype(np.int32)
+        sources[5] = sources[6]  # two queries from the same source
+        with GASBatch() as b:
+            b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+            b.set_config(chunk, 0, graphs_on)
+            for program in (PROGRAM_BFS, PROGRAM_SSSP):
+                got, _ = b.run(program, sources)
+                again, _ = b.run(program, sources)  # graph replay / reuse
+                assert np.array_equal(got, again)
+                check_queries(port, g, program, sources, got)
+
+
+def test_batch_autotune_and_errors(gpu):
+    from vertexapi2_gb300 import GasError
+    g = graphs.rmat(10, 8, seed=44, symmetrize=True, weights=(1, 9))
+    with GASBatch() as b:
+        b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+        chunk, blocks = b.autotune(PROGRAM_SSSP, 64)
+        assert chunk in (32, 128, 512, 2048) and blocks in (0, 1, 2)
+        with pytest.raises(GasError):
+            b.run(PROGRAM_SSSP, np.array([g.n_vertices], np.int32))
+        with pytest.raises(GasError):
+            b.run(3, np.array([0], np.int32))  # CC is not batched
+    with GASBatch() as b:
+        b.set_graph(g.n_vertices, g.srcs, g.dsts)  # no weights
+        with pytest.raises(GasError):
+            b.run(PROGRAM_SSSP, np.array([0], np.int32))

@@ -69,6 +69,13 @@ SIGNATURES = {
     "gas_engine_set_dense_policy": (_I32, [_P, _I32]),
     "gas_engine_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
     "gas_bfs_noalloc": (_I32, [_I32, _I32, _P, _P, _I32, _P, _P, _PI32]),
+    "gas_batch_create": (_I32, [_I32, _P, C.POINTER(_P)]),
+    "gas_batch_destroy": (_I32, [_P]),
+    "gas_batch_set_graph": (_I32, [_P, _I32, _I32, _PI32, _PI32, _PI32]),
+    "gas_batch_run": (_I32, [_P, _I32, _I32, _PI32, _PI32, _PI32]),
+    "gas_batch_set_config": (_I32, [_P, _I32, _I32, _I32]),
+    "gas_batch_autotune": (_I32, [_P, _I32, _I32, _PI32, _PI32]),
+    "gas_batch_last_ms": (_I32, [_P, C.POINTER(C.c_float)]),
     # diagnostics
     "gas_status_string": (C.c_char_p, [_I32]),
     "gas_last_error": (C.c_char_p, []),

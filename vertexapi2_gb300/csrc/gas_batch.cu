@@ -1,0 +1,438 @@
+// Batched multi-source BFS / SSSP (gas_batch_* in gas_gb300.h).
+//
+// Many queries with their own sources on one resident graph: each batch of
+// up to 256 queries is one persistent cooperative launch (kernels in
+// gas_gb300/detail/batch.cuh), and the whole batch -- source upload, state
+// reset, the run and the query-major transpose of the results -- is
+// captured once per shape into a CUDA graph and replayed.  Work units (a
+// vertex's in-edges, hubs split into chunks) and the launch shape are
+// chosen by gas_batch_autotune.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "gas_gb300.h"
+#include "gas_gb300_core.h"
+#include "gas_gb300/detail/batch.cuh"
+#include "gas_internal.h"
+
+using gas::internal::CoreGraph;
+using gas::internal::cuda_fail;
+using gas::internal::fail;
+
+namespace {
+
+constexpr int kMaxBatch = 256;  // queries per launch (8 words of query bits)
+
+struct GraphCache {
+  int kind, W, nQ, blocksPerSM, chunk;
+  cudaGraphExec_t exec;
+};
+
+}  // namespace
+
+struct gas_batch_s {
+  gas_core *core = nullptr;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sms = 0;
+  int32_t chunk = 256;
+  int32_t blocksPerSM = 0;  // 0 = as many as fit
+  bool useGraphs = true;
+  int32_t unitChunk = 0;
+  int32_t *unitV = nullptr, *unitBeg = nullptr, *unitEnd = nullptr;
+  int32_t nUnits = 0;
+  int32_t capQ = 0;
+  int32_t *value = nullptr, *srcDev = nullptr, *outDev = nullptr;
+  unsigned *mask[3] = {nullptr, nullptr, nullptr};
+  unsigned *seen = nullptr;
+  unsigned char *ctl = nullptr;  // cnt[3] | barrier[2] | rounds | err
+  int32_t *srcPinned = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  float lastMs = 0.f;
+  std::vector<GraphCache> graphs;
+};
+
+namespace {
+
+struct CtlView {
+  unsigned long long *cnt;
+  unsigned *bar;
+  int32_t *rounds;
+  unsigned *err;
+};
+CtlView ctl_view(gas_batch *b) {
+  CtlView v;
+  v.cnt = reinterpret_cast<unsigned long long *>(b->ctl);
+  v.bar = reinterpret_cast<unsigned *>(b->ctl + 24);
+  v.rounds = reinterpret_cast<int32_t *>(b->ctl + 32);
+  v.err = reinterpret_cast<unsigned *>(b->ctl + 36);
+  return v;
+}
+constexpr size_t kCtlBytes = 64;
+
+void drop_graphs(gas_batch *b) {
+  for (auto &g : b->graphs) cudaGraphExecDestroy(g.exec);
+  b->graphs.clear();
+}
+
+void free_state(gas_batch *b) {
+  void *ps[] = {b->value, b->srcDev, b->outDev, b->mask[0], b->mask[1], b->mask[2], b->seen};
+  for (void *p : ps)
+    if (p) cudaFree(p);
+  b->value = b->srcDev = b->outDev = nullptr;
+  b->mask[0] = b->mask[1] = b->mask[2] = nullptr;
+  b->seen = nullptr;
+  b->capQ = 0;
+  drop_graphs(b);
+}
+
+void free_units(gas_batch *b) {
+  if (b->unitV) cudaFree(b->unitV);
+  if (b->unitBeg) cudaFree(b->unitBeg);
+  if (b->unitEnd) cudaFree(b->unitEnd);
+  b->unitV = b->unitBeg = b->unitEnd = nullptr;
+  b->nUnits = 0;
+  b->unitChunk = 0;
+  drop_graphs(b);
+}
+
+gas_status build_units(gas_batch *b, const CoreGraph &g, int32_t chunk) {
+  if (b->unitChunk == chunk && b->unitV) return GAS_OK;
+  free_units(b);
+  std::vector<int32_t> uv, ub, ue;
+  const std::vector<int32_t> &off = *g.hInOff;
+  for (int32_t v = 0; v < g.nV; ++v)
+    for (int32_t e = off[v]; e < off[(size_t)v + 1]; e += chunk) {
+      uv.push_back(v);
+      ub.push_back(e);
+      ue.push_back(std::min(e + chunk, off[(size_t)v + 1]));
+    }
+  const size_t n = std::max<size_t>(uv.size(), 1);
+  cudaError_t e = cudaMalloc(&b->unitV, n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->unitBeg, n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->unitEnd, n * 4);
+  if (e == cudaSuccess && !uv.empty()) {
+    cudaMemcpyAsync(b->unitV, uv.data(), uv.size() * 4, cudaMemcpyHostToDevice, b->stream);
+    cudaMemcpyAsync(b->unitBeg, ub.data(), ub.size() * 4, cudaMemcpyHostToDevice, b->stream);
+    e = cudaMemcpyAsync(b->unitEnd, ue.data(), ue.size() * 4, cudaMemcpyHostToDevice, b->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) {
+    free_units(b);
+    return cuda_fail(e, "batch work units");
+  }
+  b->nUnits = (int32_t)uv.size();
+  b->unitChunk = chunk;
+  return GAS_OK;
+}
+
+gas_status ensure_state(gas_batch *b, const CoreGraph &g, int32_t Q) {
+  if (b->capQ >= Q && b->value) return GAS_OK;
+  free_state(b);
+  const size_t V = (size_t)std::max(g.nV, 1);
+  const int W = Q / 32;
+  cudaError_t e = cudaMalloc(&b->value, V * Q * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->outDev, V * Q * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->srcDev, kMaxBatch * 4);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->mask[k], V * W * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->seen, V * W * 4);
+  if (e != cudaSuccess) {
+    free_state(b);
+    return cuda_fail(e, "batch state allocation");
+  }
+  b->capQ = Q;
+  return GAS_OK;
+}
+
+template <int W, int KIND>
+gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
+  gas::detail::BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nVertices = g.nV;
+  a.nQueries = Q;
+  a.inSources = g.inSrc;
+  a.weights = reinterpret_cast<const int32_t *>(g.edgeData);
+  a.unitV = b->unitV;
+  a.unitBeg = b->unitBeg;
+  a.unitEnd = b->unitEnd;
+  a.nUnits = b->nUnits;
+  a.value = b->value;
+  for (int k = 0; k < 3; ++k) a.mask[k] = b->mask[k];
+  a.seen = b->seen;
+  CtlView cv = ctl_view(b);
+  a.cnt = cv.cnt;
+  a.barrier = cv.bar;
+  a.errWord = cv.err;
+  a.roundsOut = cv.rounds;
+  a.maxRounds = 0;
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void *)gas::detail::batch_run_kernel<W, KIND>,
+                                              dim3(blocks), dim3(256), args, 0, b->stream);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch run launch");
+}
+
+template <int W>
+gas_status launch_run_kind(gas_batch *b, const CoreGraph &g, int kind, int32_t Q, int blocks) {
+  return kind == gas::detail::kBatchBFS ? launch_run<W, gas::detail::kBatchBFS>(b, g, Q, blocks)
+                                        : launch_run<W, gas::detail::kBatchSSSP>(b, g, Q, blocks);
+}
+
+int grid_blocks(gas_batch *b, int kind, int W) {
+  int per = 0;
+  const void *fn = nullptr;
+#define GAS_BATCH_FN(w)                                                                    \
+  if (W == w)                                                                              \
+    fn = kind == gas::detail::kBatchBFS                                                    \
+             ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS>      \
+             : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP>;
+  GAS_BATCH_FN(1) GAS_BATCH_FN(2) GAS_BATCH_FN(4) GAS_BATCH_FN(8)
+#undef GAS_BATCH_FN
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+  if (b->blocksPerSM > 0 && b->blocksPerSM < per) per = b->blocksPerSM;
+  return std::max(per, 1) * std::max(b->sms, 1);
+}
+
+// The whole batch on b->stream: sources (from pinned staging), state reset,
+// initial values, the persistent run, query-major results in outDev.
+gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, int32_t Q) {
+  const int W = Q / 32;
+  const size_t V = (size_t)g.nV;
+  cudaError_t e = cudaMemcpyAsync(b->srcDev, b->srcPinned, sizeof(int32_t) * nQ,
+                                  cudaMemcpyHostToDevice, b->stream);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+    e = cudaMemsetAsync(b->mask[k], 0, V * W * 4, b->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->seen, 0, V * W * 4, b->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctl, 0, 40, b->stream);  // keep err
+  if (e != cudaSuccess) return cuda_fail(e, "batch reset");
+  gas::detail::batch_init_kernel<<<4 * b->sms, 256, 0, b->stream>>>(kind, g.nV, Q, b->value);
+  gas::detail::batch_sources_kernel<<<(nQ + 127) / 128, 128, 0, b->stream>>>(
+      kind, nQ, Q, W, b->srcDev, b->value, b->mask[0], b->seen);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "batch init");
+  const int blocks = grid_blocks(b, kind, W);
+  gas_status st;
+  switch (W) {
+    case 1: st = launch_run_kind<1>(b, g, kind, Q, blocks); break;
+    case 2: st = launch_run_kind<2>(b, g, kind, Q, blocks); break;
+    case 4: st = launch_run_kind<4>(b, g, kind, Q, blocks); break;
+    default: st = launch_run_kind<8>(b, g, kind, Q, blocks); break;
+  }
+  if (st) return st;
+  dim3 tb(32, 8), tg((g.nV + 31) / 32, (Q + 31) / 32);
+  gas::detail::batch_transpose_kernel<<<tg, tb, 0, b->stream>>>(b->value, g.nV, Q, nQ, b->outDev);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch transpose");
+}
+
+gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const int32_t *sources,
+                   int32_t *results, int32_t *rounds) {
+  int32_t Q = 32;
+  while (Q < nQ) Q *= 2;
+  gas_status st = ensure_state(b, g, std::max(Q, 32));
+  if (st) return st;
+  memcpy(b->srcPinned, sources, sizeof(int32_t) * nQ);
+  cudaEventRecord(b->t0, b->stream);
+  bool launched = false;
+  if (b->useGraphs) {
+    cudaGraphExec_t exec = nullptr;
+    for (auto &c : b->graphs)
+      if (c.kind == kind && c.W == Q / 32 && c.nQ == nQ && c.blocksPerSM == b->blocksPerSM &&
+          c.chunk == b->unitChunk)
+        exec = c.exec;
+    if (!exec) {
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        gas_status cst = enqueue_batch(b, g, kind, nQ, Q);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+        if (cst == GAS_OK && ce == cudaSuccess && graph &&
+            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+          b->graphs.push_back({kind, Q / 32, nQ, b->blocksPerSM, b->unitChunk, exec});
+        } else {
+          exec = nullptr;
+          b->useGraphs = false;  // this runtime cannot capture the batch: launch directly
+        }
+        if (graph) cudaGraphDestroy(graph);
+      } else {
+        b->useGraphs = false;
+      }
+      cudaGetLastError();
+    }
+    if (exec) {
+      cudaError_t e = cudaGraphLaunch(exec, b->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "batch graph launch");
+      launched = true;
+    }
+  }
+  if (!launched) {
+    st = enqueue_batch(b, g, kind, nQ, Q);
+    if (st) return st;
+  }
+  cudaEventRecord(b->t1, b->stream);
+  CtlView cv = ctl_view(b);
+  int32_t re[2] = {0, 0};  // rounds, err
+  cudaError_t e = cudaMemcpyAsync(re, cv.rounds, 8, cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess && results)
+    e = cudaMemcpyAsync(results, b->outDev, sizeof(int32_t) * (size_t)nQ * g.nV,
+                        cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "batch run");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->t0, b->t1);
+  b->lastMs += ms;
+  if (re[1]) {
+    cudaMemsetAsync(cv.err, 0, 4, b->stream);
+    return fail(GAS_ERR_TIMEOUT, "a bounded device wait of the batched run timed out");
+  }
+  if (rounds) *rounds = std::max(*rounds, re[0]);
+  return GAS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gas_status gas_batch_create(int32_t device, void *stream, gas_batch **out) {
+  if (!out) return fail(GAS_ERR_INVALID, "gas_batch_create: out is NULL");
+  *out = nullptr;
+  gas_batch *b = new (std::nothrow) gas_batch_s();
+  if (!b) return fail(GAS_ERR_OOM, "host allocation");
+  gas_status st = gas_core_create(device, stream, &b->core);
+  if (st) {
+    delete b;
+    return st;
+  }
+  b->device = device;
+  b->stream = (cudaStream_t)stream;
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+  cudaError_t e = cudaMalloc(&b->ctl, kCtlBytes);
+  if (e == cudaSuccess) e = cudaMemset(b->ctl, 0, kCtlBytes);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->srcPinned, sizeof(int32_t) * kMaxBatch);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+  if (e != cudaSuccess) {
+    gas_batch_destroy(b);
+    return cuda_fail(e, "batch creation");
+  }
+  *out = b;
+  return GAS_OK;
+}
+
+gas_status gas_batch_destroy(gas_batch *b) {
+  if (!b) return GAS_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  free_state(b);
+  free_units(b);
+  if (b->ctl) cudaFree(b->ctl);
+  if (b->srcPinned) cudaFreeHost(b->srcPinned);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
+  gas_core_destroy(b->core);
+  delete b;
+  return GAS_OK;
+}
+
+gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
+                               const int32_t *srcs, const int32_t *dsts, const int32_t *weights) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  cudaSetDevice(b->device);
+  free_state(b);
+  free_units(b);
+  gas_status st = gas_core_set_graph(b->core, nVertices, nEdges, srcs, dsts, weights,
+                                     weights ? 4 : 0, 4, 4);
+  if (st) return st;
+  CoreGraph g;
+  gas::internal::core_graph(b->core, &g);
+  return build_units(b, g, b->chunk);
+}
+
+gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocksPerSM,
+                                int32_t useGraphs) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  if (chunkEdges < 1 || blocksPerSM < 0) return fail(GAS_ERR_INVALID, "bad batch config");
+  b->chunk = chunkEdges;
+  b->blocksPerSM = blocksPerSM;
+  b->useGraphs = useGraphs != 0;
+  drop_graphs(b);
+  CoreGraph g;
+  if (gas::internal::core_graph(b->core, &g)) return build_units(b, g, chunkEdges);
+  return GAS_OK;
+}
+
+gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries, const int32_t *sources,
+                         int32_t *results, int32_t *rounds) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  CoreGraph g;
+  if (!gas::internal::core_graph(b->core, &g)) return fail(GAS_ERR_STATE, "no graph set");
+  int kind;
+  if (program == GAS_PROGRAM_BFS) {
+    kind = gas::detail::kBatchBFS;
+  } else if (program == GAS_PROGRAM_SSSP) {
+    kind = gas::detail::kBatchSSSP;
+    if (g.edgeBytes != 4 || !g.edgeData)
+      return fail(GAS_ERR_STATE, "batched SSSP needs int32 edge weights in setGraph");
+  } else {
+    return fail(GAS_ERR_UNSUPPORTED, "batched runs support BFS and SSSP");
+  }
+  if (nQueries < 0 || (nQueries > 0 && !sources)) return fail(GAS_ERR_INVALID, "bad sources");
+  for (int32_t q = 0; q < nQueries; ++q)
+    if (sources[q] < 0 || sources[q] >= g.nV)
+      return fail(GAS_ERR_INVALID, "source %d of query %d outside [0, %d)", sources[q], q, g.nV);
+  cudaSetDevice(b->device);
+  b->lastMs = 0.f;
+  if (rounds) *rounds = 0;
+  for (int32_t q0 = 0; q0 < nQueries; q0 += kMaxBatch) {
+    const int32_t nq = std::min(kMaxBatch, nQueries - q0);
+    gas_status st = run_one(b, g, kind, nq, sources + q0,
+                            results ? results + (size_t)q0 * g.nV : nullptr, rounds);
+    if (st) return st;
+  }
+  return GAS_OK;
+}
+
+gas_status gas_batch_last_ms(gas_batch *b, float *ms) {
+  if (!b || !ms) return fail(GAS_ERR_INVALID, "null argument");
+  *ms = b->lastMs;
+  return GAS_OK;
+}
+
+gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
+                              int32_t *chunkOut, int32_t *blocksOut) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  CoreGraph g;
+  if (!gas::internal::core_graph(b->core, &g)) return fail(GAS_ERR_STATE, "no graph set");
+  const int32_t nq = std::max(1, std::min(nQueries, kMaxBatch));
+  std::vector<int32_t> src(nq);
+  std::mt19937 rng(12345);
+  for (auto &s : src) s = (int32_t)(rng() % (uint32_t)std::max(g.nV, 1));
+  const int32_t chunks[] = {32, 128, 512, 2048};
+  const int32_t blocks[] = {0, 2, 1};
+  float best = 1e30f;
+  int32_t bc = b->chunk, bb = b->blocksPerSM;
+  for (int32_t c : chunks)
+    for (int32_t k : blocks) {
+      gas_status st = gas_batch_set_config(b, c, k, b->useGraphs ? 1 : 0);
+      if (st) return st;
+      int32_t r = 0;
+      st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);  // warm (and capture)
+      if (st) return st;
+      st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);
+      if (st) return st;
+      if (b->lastMs < best) {
+        best = b->lastMs;
+        bc = c;
+        bb = k;
+      }
+    }
+  gas_status st = gas_batch_set_config(b, bc, bb, b->useGraphs ? 1 : 0);
+  if (chunkOut) *chunkOut = bc;
+  if (blocksOut) *blocksOut = bb;
+  return st;
+}
+
+}  // extern "C"

@@ -275,6 +275,27 @@ gas_status check_device_error(gas_core *c) {
 
 }  // namespace
 
+namespace gas {
+namespace internal {
+bool core_graph(gas_core_s *c, CoreGraph *out) {
+  if (!c || !c->haveGraph) return false;
+  out->device = c->device;
+  out->stream = c->stream;
+  out->nV = c->nV;
+  out->nE = c->nE;
+  out->inOff = c->inOff;
+  out->inSrc = c->inSrc;
+  out->outOff = c->outOff;
+  out->outDst = c->outDst;
+  out->edgeData = c->ed;
+  out->edgeBytes = c->edgeBytes;
+  out->hInOff = &c->hInOff;
+  out->hOutOff = &c->hOutOff;
+  return true;
+}
+}  // namespace internal
+}  // namespace gas
+
 extern "C" {
 
 gas_status gas_core_create(int32_t device, void *stream, gas_core **out) {

@@ -22,5 +22,19 @@ void build_adjacency(int32_t nV, int32_t nE, const int32_t *key, const int32_t *
                      std::vector<int32_t> &off, std::vector<int32_t> &adj,
                      std::vector<int32_t> *perm);
 
+// Device graph of a gas_core (CSC, CSR, edge data in CSC order), for the
+// other engines of the library that share its graph build.
+struct CoreGraph {
+  int device;
+  cudaStream_t stream;
+  int32_t nV, nE;
+  const int32_t *inOff, *inSrc, *outOff, *outDst;
+  const void *edgeData;
+  int32_t edgeBytes;
+  const std::vector<int32_t> *hInOff;
+  const std::vector<int32_t> *hOutOff;
+};
+bool core_graph(struct gas_core_s *c, CoreGraph *out);
+
 }  // namespace internal
 }  // namespace gas

@@ -152,3 +152,65 @@ class GASEngine:
 
 def device_supported(device: int = 0) -> bool:
     return bool(load().gas_device_supported(device))
+
+
+class GASBatch:
+    """Batched multi-source BFS / SSSP on one resident graph (gas_batch_*)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._lib = load()
+        h = C.c_void_p()
+        check(self._lib.gas_batch_create(device, C.c_void_p(stream or 0), C.byref(h)),
+              "gas_batch_create")
+        self._h = h
+        self.n_vertices = 0
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gas_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_graph(self, n_vertices: int, srcs, dsts, weights=None) -> None:
+        s = np.ascontiguousarray(srcs, dtype=np.int32)
+        d = np.ascontiguousarray(dsts, dtype=np.int32)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.int32)
+        check(self._lib.gas_batch_set_graph(self._h, n_vertices, int(s.shape[0]), _i32ptr(s),
+                                            _i32ptr(d), _i32ptr(w) if w is not None else None),
+              "gas_batch_set_graph")
+        self.n_vertices = n_vertices
+
+    def run(self, program: int, sources, want_results: bool = True):
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        out = np.empty((src.shape[0], self.n_vertices), dtype=np.int32) if want_results else None
+        rounds = C.c_int32()
+        check(self._lib.gas_batch_run(self._h, program, int(src.shape[0]), _i32ptr(src),
+                                      _i32ptr(out) if out is not None else None, C.byref(rounds)),
+              "gas_batch_run")
+        return out, rounds.value
+
+    def set_config(self, chunk_edges: int = 256, blocks_per_sm: int = 0, use_graphs: bool = True):
+        check(self._lib.gas_batch_set_config(self._h, chunk_edges, blocks_per_sm, int(use_graphs)),
+              "gas_batch_set_config")
+
+    def autotune(self, program: int, n_queries: int) -> tuple[int, int]:
+        c, b = C.c_int32(), C.c_int32()
+        check(self._lib.gas_batch_autotune(self._h, program, n_queries, C.byref(c), C.byref(b)),
+              "gas_batch_autotune")
+        return c.value, b.value
+
+    def last_ms(self) -> float:
+        ms = C.c_float()
+        check(self._lib.gas_batch_last_ms(self._h, C.byref(ms)), "gas_batch_last_ms")
+        return float(ms.value)
