@@ -46,6 +46,9 @@ WORKLOADS = {
     "bfs-rmat16": dict(desc="BFS, R-MAT scale 16 ef 16 (0.57/0.19/0.19), symmetrised, source = max out-degree"),
     "pagerank-rmat22": dict(desc="PageRank FP32 (0.85, tol 0.01, <=50 rounds), R-MAT scale 22 ef 16, directed"),
     "cc-rmat22": dict(desc="connected components, R-MAT scale 22 ef 16, symmetrised"),
+    "batch-c4": dict(desc="256 BFS + 256 SSSP queries, uniform random sources, on R-MAT scale 21 "
+                          "ef 16 symmetrised (w in [1,255]) and on the 1024x1024 lattice; batched "
+                          "engine vs one-at-a-time plain runs"),
 }
 SEED = 1
 RMAT_SCALE = {"pagerank-rmat22": 22, "cc-rmat22": 22}
@@ -394,6 +397,96 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_batch_c4(args):
+    """Batched multi-source queries (queries/s) vs one-at-a-time plain runs."""
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    import vertexapi2_gb300 as gas
+    from vertexapi2_gb300 import graphs
+    from vertexapi2_gb300 import programs as P
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
+    gas.load()
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(SEED)
+    nq = 256
+    gs = [("rmat21", graphs.rmat(21, 16, seed=SEED, symmetrize=True, weights=(1, 255))),
+          ("grid1024", graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100)))]
+    sets = []
+    for name, g in gs:
+        b = gas.GASBatch(device=local, stream=stream.cuda_stream)
+        b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+        tuned = {}
+        for prog in (PROGRAM_BFS, PROGRAM_SSSP):
+            src = rng.integers(0, g.n_vertices, nq).astype(np.int32)
+            tuned[prog] = b.autotune(prog, nq)
+            sets.append((name, g, b, prog, src, tuned[prog]))
+    def batched_step():
+        ms = 0.0
+        for name, g, b, prog, src, cfg in sets:
+            b.set_config(cfg[0], cfg[1], True)
+            b.run(prog, src, want_results=False)
+            ms += b.last_ms()
+        return ms
+    for _ in range(args.warmup):
+        batched_step()
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        step_ms = [batched_step() for _ in range(args.steps)]
+    total_ms = allreduce_max(world, float(sum(step_ms)))
+    queries = allreduce_sum(world, float(len(sets) * nq * args.steps))
+    value = queries / (total_ms / 1e3)
+    # end to end: results of every query copied to host memory each step
+    t0 = time.perf_counter()
+    for name, g, b, prog, src, cfg in sets:
+        b.set_config(cfg[0], cfg[1], True)
+        b.run(prog, src, want_results=True)
+    e2e_s = time.perf_counter() - t0
+    e2e_value = len(sets) * nq / e2e_s
+    d2h = sum(nq * g.n_vertices * 4 for _, g, _, _, _, _ in sets)
+    # one-at-a-time plain engine on a sample of the same queries
+    sample = 8
+    single_ms, single_n = 0.0, 0
+    parity = True
+    for name, g, b, prog, src, cfg in sets:
+        batch_out, _ = b.run(prog, src[:sample])
+        e = gas.GASEngine(prog, device=local, stream=stream.cuda_stream)
+        for q, s0 in enumerate(src[:sample]):
+            vd = P.bfs_init(g.n_vertices) if prog == PROGRAM_BFS else P.sssp_init(g.n_vertices, int(s0))
+            e.set_graph(g.n_vertices, vd, g.srcs, g.dsts, g.weights if prog == PROGRAM_SSSP else None) \
+                if q == 0 else e.set_vertex_data(vd)
+            act = (int(s0), int(s0) + 1) if prog == PROGRAM_BFS else (0, g.n_vertices)
+            e.set_active(*act)
+            e.run()
+            single_ms += e.last_run_ms()
+            single_n += 1
+            e.get_results()  # into the array borrowed by set_graph
+            parity &= bool(np.array_equal(e.vertex_data, batch_out[q]))
+        e.close()
+    single_qps = single_n / (single_ms / 1e3)
+    if rank != 0:
+        return
+    line = {
+        "metric": "batched queries/s (vs one-at-a-time plain engine)", "value": value,
+        "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": "batch-c4", "desc": WORKLOADS["batch-c4"]["desc"], "seed": SEED,
+                   "queries_per_step": len(sets) * nq,
+                   "autotuned": {f"{n}-{'bfs' if p == PROGRAM_BFS else 'sssp'}": list(c)
+                                 for n, _, _, p, _, c in sets},
+                   "l2": "inputs (R-MAT-21 CSC/CSR, 2 GB query state) larger than L2"},
+        "one_at_a_time": {"value": single_qps, "unit": "queries/s", "sample_queries": single_n,
+                          "speedup": value / single_qps, "results_identical": parity},
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * nq * len(sets),
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": 5 * len(sets) * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -410,6 +503,8 @@ def main():
             RMAT_SCALE[k] = args.rmat_scale
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch-c4":
+        run_batch_c4(args)
     else:
         run_ours(args)
 
