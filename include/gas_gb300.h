@@ -212,6 +212,11 @@ GAS_API gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_
  * the fastest; reports the chosen chunk size and CTAs per SM. */
 GAS_API gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
                                       int32_t *chunkEdges, int32_t *blocksPerSM);
+/* Round policy: a round pushes from the vertices that changed last round
+ * when their out-degree total times alpha is at most nEdges, otherwise it
+ * pulls over every vertex (default alpha 10; 0 = always push).  Results do
+ * not depend on it. */
+GAS_API gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha);
 /* Device milliseconds of the most recent gas_batch_run. */
 GAS_API gas_status gas_batch_last_ms(gas_batch *b, float *ms);
 

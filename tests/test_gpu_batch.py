@@ -34,8 +34,9 @@ def test_batch_matches_single_source_rmat(gpu, port, nq):
             check_queries(port, g, program, sources[: min(nq, 64)], got)
 
 
-@pytest.mark.parametrize("chunk,graphs_on", [(1, True), (32, False), (2048, True)])
-def test_batch_configs_directed_and_grid(gpu, port, chunk, graphs_on):
+@pytest.mark.parametrize("chunk,graphs_on,alpha", [(1, True, 10), (32, False, 0),
+                                                   (2048, True, 1 << 20), (128, True, 2)])
+def test_batch_configs_directed_and_grid(gpu, port, chunk, graphs_on, alpha):
     for g in (graphs.rmat(11, 16, seed=42, weights=(1, 100)),
               graphs.grid(48, 40, 0.15, seed=43)):
         rng = np.random.default_rng(chunk)
@@ -44,6 +45,7 @@ def test_batch_configs_directed_and_grid(gpu, port, chunk, graphs_on):
         with GASBatch() as b:
             b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
             b.set_config(chunk, 0, graphs_on)
+            b.set_policy(alpha)
             for program in (PROGRAM_BFS, PROGRAM_SSSP):
                 got, _ = b.run(program, sources)
                 again, _ = b.run(program, sources)  # graph replay / reuse

@@ -76,6 +76,7 @@ SIGNATURES = {
     "gas_batch_set_config": (_I32, [_P, _I32, _I32, _I32]),
     "gas_batch_autotune": (_I32, [_P, _I32, _I32, _PI32, _PI32]),
     "gas_batch_last_ms": (_I32, [_P, C.POINTER(C.c_float)]),
+    "gas_batch_set_policy": (_I32, [_P, _I32]),
     # diagnostics
     "gas_status_string": (C.c_char_p, [_I32]),
     "gas_last_error": (C.c_char_p, []),

@@ -43,7 +43,11 @@ struct gas_batch_s {
   int32_t chunk = 256;
   int32_t blocksPerSM = 0;  // 0 = as many as fit
   bool useGraphs = true;
+  int32_t alpha = 10;  // push round when list out-degree total * alpha <= E
   int32_t unitChunk = 0;
+  int32_t *list[3] = {nullptr, nullptr, nullptr};
+  int32_t *inList = nullptr;
+  int32_t *weightsOut = nullptr;  // CSR order
   int32_t *unitV = nullptr, *unitBeg = nullptr, *unitEnd = nullptr;
   int32_t nUnits = 0;
   int32_t capQ = 0;
@@ -59,11 +63,13 @@ struct gas_batch_s {
 
 namespace {
 
+// control block: cnt[3] | barrier[2] | rounds | err | listCnt[3]
 struct CtlView {
   unsigned long long *cnt;
   unsigned *bar;
   int32_t *rounds;
   unsigned *err;
+  unsigned long long *listCnt;
 };
 CtlView ctl_view(gas_batch *b) {
   CtlView v;
@@ -71,6 +77,7 @@ CtlView ctl_view(gas_batch *b) {
   v.bar = reinterpret_cast<unsigned *>(b->ctl + 24);
   v.rounds = reinterpret_cast<int32_t *>(b->ctl + 32);
   v.err = reinterpret_cast<unsigned *>(b->ctl + 36);
+  v.listCnt = reinterpret_cast<unsigned long long *>(b->ctl + 40);
   return v;
 }
 constexpr size_t kCtlBytes = 64;
@@ -81,12 +88,15 @@ void drop_graphs(gas_batch *b) {
 }
 
 void free_state(gas_batch *b) {
-  void *ps[] = {b->value, b->srcDev, b->outDev, b->mask[0], b->mask[1], b->mask[2], b->seen};
+  void *ps[] = {b->value, b->srcDev, b->outDev, b->mask[0], b->mask[1], b->mask[2], b->seen,
+                b->list[0], b->list[1], b->list[2], b->inList};
   for (void *p : ps)
     if (p) cudaFree(p);
   b->value = b->srcDev = b->outDev = nullptr;
   b->mask[0] = b->mask[1] = b->mask[2] = nullptr;
   b->seen = nullptr;
+  b->list[0] = b->list[1] = b->list[2] = nullptr;
+  b->inList = nullptr;
   b->capQ = 0;
   drop_graphs(b);
 }
@@ -141,6 +151,8 @@ gas_status ensure_state(gas_batch *b, const CoreGraph &g, int32_t Q) {
   if (e == cudaSuccess) e = cudaMalloc(&b->srcDev, kMaxBatch * 4);
   for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->mask[k], V * W * 4);
   if (e == cudaSuccess) e = cudaMalloc(&b->seen, V * W * 4);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->list[k], V * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&b->inList, V * 4);
   if (e != cudaSuccess) {
     free_state(b);
     return cuda_fail(e, "batch state allocation");
@@ -154,6 +166,13 @@ gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
   gas::detail::BatchArgs a;
   memset(&a, 0, sizeof(a));
   a.nVertices = g.nV;
+  a.nEdges = g.nE;
+  a.outOffsets = g.outOff;
+  a.outDests = g.outDst;
+  a.weightsOut = b->weightsOut;
+  for (int k = 0; k < 3; ++k) a.list[k] = b->list[k];
+  a.inList = b->inList;
+  a.alpha = b->alpha;
   a.nQueries = Q;
   a.inSources = g.inSrc;
   a.weights = reinterpret_cast<const int32_t *>(g.edgeData);
@@ -169,6 +188,7 @@ gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
   a.barrier = cv.bar;
   a.errWord = cv.err;
   a.roundsOut = cv.rounds;
+  a.listCnt = cv.listCnt;
   a.maxRounds = 0;
   void *args[] = {&a};
   cudaError_t e = cudaLaunchCooperativeKernel((const void *)gas::detail::batch_run_kernel<W, KIND>,
@@ -207,11 +227,14 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
   for (int k = 0; k < 3 && e == cudaSuccess; ++k)
     e = cudaMemsetAsync(b->mask[k], 0, V * W * 4, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->seen, 0, V * W * 4, b->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctl, 0, 40, b->stream);  // keep err
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->inList, 0xff, V * 4, b->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctl, 0, kCtlBytes, b->stream);
   if (e != cudaSuccess) return cuda_fail(e, "batch reset");
   gas::detail::batch_init_kernel<<<4 * b->sms, 256, 0, b->stream>>>(kind, g.nV, Q, b->value);
+  CtlView cv = ctl_view(b);
   gas::detail::batch_sources_kernel<<<(nQ + 127) / 128, 128, 0, b->stream>>>(
-      kind, nQ, Q, W, b->srcDev, b->value, b->mask[0], b->seen);
+      kind, nQ, Q, W, b->srcDev, b->value, b->mask[0], b->seen, g.outOff, b->inList,
+      b->list[0], cv.listCnt);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch init");
   const int blocks = grid_blocks(b, kind, W);
@@ -328,6 +351,7 @@ gas_status gas_batch_destroy(gas_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   free_state(b);
   free_units(b);
+  if (b->weightsOut) cudaFree(b->weightsOut);
   if (b->ctl) cudaFree(b->ctl);
   if (b->srcPinned) cudaFreeHost(b->srcPinned);
   if (b->t0) cudaEventDestroy(b->t0);
@@ -343,12 +367,23 @@ gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
   cudaSetDevice(b->device);
   free_state(b);
   free_units(b);
+  if (b->weightsOut) cudaFree(b->weightsOut);
+  b->weightsOut = nullptr;
   gas_status st = gas_core_set_graph(b->core, nVertices, nEdges, srcs, dsts, weights,
                                      weights ? 4 : 0, 4, 4);
   if (st) return st;
   CoreGraph g;
   gas::internal::core_graph(b->core, &g);
-  return build_units(b, g, b->chunk);
+  st = build_units(b, g, b->chunk);
+  if (st || !weights || nEdges == 0) return st;
+  // weights in CSR order for push rounds (stable by source, as the CSR)
+  std::vector<int32_t> off, wcsr;
+  gas::internal::build_adjacency(nVertices, nEdges, srcs, weights, off, wcsr, nullptr);
+  cudaError_t e = cudaMalloc(&b->weightsOut, sizeof(int32_t) * (size_t)nEdges);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->weightsOut, wcsr.data(), sizeof(int32_t) * (size_t)nEdges,
+                   cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch CSR weights");
 }
 
 gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocksPerSM,
@@ -392,6 +427,14 @@ gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries, const 
                             results ? results + (size_t)q0 * g.nV : nullptr, rounds);
     if (st) return st;
   }
+  return GAS_OK;
+}
+
+gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  if (alpha < 0) return fail(GAS_ERR_INVALID, "alpha must be >= 0");
+  b->alpha = alpha;
+  drop_graphs(b);
   return GAS_OK;
 }
 

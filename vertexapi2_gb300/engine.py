@@ -204,6 +204,9 @@ class GASBatch:
         check(self._lib.gas_batch_set_config(self._h, chunk_edges, blocks_per_sm, int(use_graphs)),
               "gas_batch_set_config")
 
+    def set_policy(self, alpha: int) -> None:
+        check(self._lib.gas_batch_set_policy(self._h, alpha), "gas_batch_set_policy")
+
     def autotune(self, program: int, n_queries: int) -> tuple[int, int]:
         c, b = C.c_int32(), C.c_int32()
         check(self._lib.gas_batch_autotune(self._h, program, n_queries, C.byref(c), C.byref(b)),
