@@ -220,6 +220,91 @@ GAS_API gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha);
 /* Device milliseconds of the most recent gas_batch_run. */
 GAS_API gas_status gas_batch_last_ms(gas_batch *b, float *ms);
 
+/* ---------------- serving loop ------------------------------------------ */
+/* A request loop over graphs kept resident on one device (no counterpart in
+ * the reference).  Queries -- BFS, SSSP or personalised PageRank (PPR:
+ * alpha 0.15, teleport to the source, 20 rounds) from one source on one
+ * resident graph -- are submitted at any time from any thread.  A
+ * scheduler thread batches the queries waiting for the same graph and
+ * program into one batch (up to maxBatch queries) whenever one of `lanes`
+ * streams is free and device memory admits it, and advances every batch in
+ * flight round by round, so batches on different lanes share the device
+ * and new queries start while others run (continuous batching).
+ *
+ * Admission by free device memory: a batch of Q queries needs working
+ * state of (BFS) V*Q*4 + V*(Q/8)*4 + 16*V bytes, (SSSP) V*Q*4 + V*(Q/32)*12
+ * + 16*V, (PPR) V*Q*16 + 2*V, plus V*nQ*4 for its results.  It starts only
+ * when cudaMemGetInfo's free bytes plus the server pool's cached bytes,
+ * minus reserveBytes, cover it; otherwise the batch shrinks (in steps of
+ * 32 queries) or waits for a running batch to release memory.  A query
+ * that cannot fit even alone on an idle device fails with GAS_ERR_OOM.
+ *
+ * Results: BFS depth (-1 unreached) and SSSP distance (2147383647
+ * unreached) as int32, PPR rank as float, nVertices values per query; each
+ * equals the query's single-source result (BFS, SSSP: bit for bit with
+ * gas_engine_run; PPR: bit for bit with the reference engine's CPU loop in
+ * FP32) whatever the batch it ran in.  They stay in device memory until
+ * gas_server_wait fetches them. */
+typedef struct gas_server_s gas_server;
+
+typedef struct {
+  int32_t lanes;         /* batches in flight at once, one stream each (1..16; default 4) */
+  int32_t maxBatch;      /* queries per batch (1..256; default 256)                     */
+  int64_t reserveBytes;  /* device memory admission leaves free (default 1 GiB)          */
+} gas_server_config;
+
+typedef struct {
+  int32_t status;     /* gas_status of the query                           */
+  int32_t program;
+  int32_t graph;
+  int32_t source;
+  int32_t rounds;     /* rounds its batch ran                              */
+  int32_t batchSize;  /* queries in that batch                             */
+  int32_t lane;
+  int32_t pad;
+  int64_t submitNs;   /* steady-clock nanoseconds: submitted, batch        */
+  int64_t admitNs;    /* admitted, results complete in device memory        */
+  int64_t doneNs;
+} gas_query_info;
+
+typedef struct {
+  int64_t submitted, completed, failed;
+  int64_t batches;           /* batches started                               */
+  int64_t batchedQueries;    /* queries in them (mean batch = this / batches) */
+  int64_t memoryWaits;       /* admissions deferred or shrunk for memory      */
+  int64_t bytesInUse;        /* device bytes held by batches and results      */
+  int64_t peakBytesInUse;
+  int64_t pending;           /* queries submitted and not yet in a batch      */
+  int64_t running;           /* batches in flight                              */
+} gas_server_stats;
+
+/* cfg may be NULL (defaults).  Starts the scheduler thread. */
+GAS_API gas_status gas_server_create(int32_t device, const gas_server_config *cfg,
+                                     gas_server **out);
+/* Stops the scheduler after the batches in flight; queries not yet started
+ * and results not yet fetched are dropped. */
+GAS_API gas_status gas_server_destroy(gas_server *s);
+/* Uploads a graph (edge list as gas_engine_set_graph; int32 weights, may be
+ * NULL, are the SSSP edge lengths) and keeps it resident; GAS_ERR_OOM when
+ * it does not fit in free device memory minus reserveBytes. */
+GAS_API gas_status gas_server_add_graph(gas_server *s, int32_t nVertices, int32_t nEdges,
+                                        const int32_t *srcs, const int32_t *dsts,
+                                        const int32_t *weights, int32_t *graphId);
+/* Non-blocking.  program = GAS_PROGRAM_BFS, _SSSP (graph with weights) or
+ * _PPR. */
+GAS_API gas_status gas_server_submit(gas_server *s, int32_t graphId, int32_t program,
+                                     int32_t source, uint64_t *ticket);
+/* Waits up to timeoutMs (< 0: no limit) for the query; GAS_ERR_TIMEOUT if
+ * it is still running (wait again later).  On completion copies its
+ * nVertices results into `result` (host memory of resultBytes, may be
+ * NULL), fills `info` (may be NULL), releases the query and returns the
+ * query's own status. */
+GAS_API gas_status gas_server_wait(gas_server *s, uint64_t ticket, int32_t timeoutMs,
+                                   void *result, int64_t resultBytes, gas_query_info *info);
+/* *done = 1 when the query has completed (successfully or not). */
+GAS_API gas_status gas_server_poll(gas_server *s, uint64_t ticket, int32_t *done);
+GAS_API gas_status gas_server_get_stats(gas_server *s, gas_server_stats *st);
+
 /* ---------------- status / diagnostics ---------------------------------- */
 GAS_API const char *gas_status_string(gas_status s);
 GAS_API const char *gas_last_error(void);

@@ -123,3 +123,22 @@ def test_engine_without_device_reports_no_device(gas_lib):
         pytest.skip("a device is present")
     h = C.c_void_p()
     assert gas_lib.gas_engine_create(1, 0, None, C.byref(h)) == 7
+    b = C.c_void_p()
+    assert gas_lib.gas_batch_create(0, None, C.byref(b)) != 0
+
+
+def test_server_argument_and_device_errors(gas_lib):
+    """Configuration is checked before the device; without a device the
+    server reports GAS_ERR_NO_DEVICE and hands out nothing."""
+    import ctypes as C
+    from vertexapi2_gb300._lib import ServerConfig
+    h = C.c_void_p()
+    assert gas_lib.gas_server_create(0, C.byref(ServerConfig(0, 256, 0)), C.byref(h)) == 1
+    assert gas_lib.gas_server_create(0, C.byref(ServerConfig(4, 257, 0)), C.byref(h)) == 1
+    assert gas_lib.gas_server_create(0, C.byref(ServerConfig(4, 256, -1)), C.byref(h)) == 1
+    assert gas_lib.gas_server_create(0, None, None) == 1
+    assert gas_lib.gas_server_destroy(None) == 0
+    assert gas_lib.gas_server_submit(None, 0, 1, 0, None) == 1
+    if not gas_lib.gas_device_supported(0):
+        assert gas_lib.gas_server_create(0, None, C.byref(h)) == 7
+        assert not h.value

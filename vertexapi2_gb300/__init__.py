@@ -7,7 +7,7 @@ benchmark.
 """
 from ._lib import (GasError, PROGRAM_BFS, PROGRAM_CC, PROGRAM_PAGERANK, PROGRAM_PPR,
                    PROGRAM_SSSP, load)
-from .engine import GASBatch, GASEngine, device_supported
+from .engine import GASBatch, GASEngine, GASServer, device_supported
 
-__all__ = ["GASEngine", "GASBatch", "GasError", "load", "device_supported", "PROGRAM_BFS", "PROGRAM_SSSP",
+__all__ = ["GASEngine", "GASBatch", "GASServer", "GasError", "load", "device_supported", "PROGRAM_BFS", "PROGRAM_SSSP",
            "PROGRAM_CC", "PROGRAM_PAGERANK", "PROGRAM_PPR"]

@@ -40,6 +40,23 @@ class EdgeList(C.Structure):
                 ("weights", C.POINTER(C.c_int32))]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("lanes", C.c_int32), ("maxBatch", C.c_int32), ("reserveBytes", C.c_int64)]
+
+
+class QueryInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("program", C.c_int32), ("graph", C.c_int32),
+                ("source", C.c_int32), ("rounds", C.c_int32), ("batchSize", C.c_int32),
+                ("lane", C.c_int32), ("pad", C.c_int32), ("submitNs", C.c_int64),
+                ("admitNs", C.c_int64), ("doneNs", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in (
+        "submitted", "completed", "failed", "batches", "batchedQueries", "memoryWaits",
+        "bytesInUse", "peakBytesInUse", "pending", "running")]
+
+
 _P = C.c_void_p
 _I32 = C.c_int32
 _PI32 = C.POINTER(C.c_int32)
@@ -77,6 +94,14 @@ SIGNATURES = {
     "gas_batch_autotune": (_I32, [_P, _I32, _I32, _PI32, _PI32]),
     "gas_batch_last_ms": (_I32, [_P, C.POINTER(C.c_float)]),
     "gas_batch_set_policy": (_I32, [_P, _I32]),
+    # serving loop
+    "gas_server_create": (_I32, [_I32, C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "gas_server_destroy": (_I32, [_P]),
+    "gas_server_add_graph": (_I32, [_P, _I32, _I32, _PI32, _PI32, _PI32, _PI32]),
+    "gas_server_submit": (_I32, [_P, _I32, _I32, _I32, C.POINTER(C.c_uint64)]),
+    "gas_server_wait": (_I32, [_P, C.c_uint64, _I32, _P, C.c_int64, C.POINTER(QueryInfo)]),
+    "gas_server_poll": (_I32, [_P, C.c_uint64, _PI32]),
+    "gas_server_get_stats": (_I32, [_P, C.POINTER(ServerStats)]),
     # diagnostics
     "gas_status_string": (C.c_char_p, [_I32]),
     "gas_last_error": (C.c_char_p, []),

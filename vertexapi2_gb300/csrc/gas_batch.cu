@@ -317,6 +317,20 @@ gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const
 
 }  // namespace
 
+namespace gas {
+namespace internal {
+bool batch_graph(gas_batch_s *b, BatchGraph *out) {
+  if (!b || !core_graph(b->core, &out->g)) return false;
+  out->weightsOut = b->weightsOut;
+  out->unitV = b->unitV;
+  out->unitBeg = b->unitBeg;
+  out->unitEnd = b->unitEnd;
+  out->nUnits = b->nUnits;
+  return true;
+}
+}  // namespace internal
+}  // namespace gas
+
 extern "C" {
 
 gas_status gas_batch_create(int32_t device, void *stream, gas_batch **out) {

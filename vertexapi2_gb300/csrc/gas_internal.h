@@ -36,5 +36,15 @@ struct CoreGraph {
 };
 bool core_graph(struct gas_core_s *c, CoreGraph *out);
 
+// A gas_batch's graph with its batched-run extras: out-edge weights in CSR
+// order and the pull work units (a vertex's in-edges, hubs in chunks).
+struct BatchGraph {
+  CoreGraph g;
+  const int32_t *weightsOut;
+  const int32_t *unitV, *unitBeg, *unitEnd;
+  int32_t nUnits;
+};
+bool batch_graph(struct gas_batch_s *b, BatchGraph *out);
+
 }  // namespace internal
 }  // namespace gas

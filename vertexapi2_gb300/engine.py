@@ -217,3 +217,86 @@ class GASBatch:
         ms = C.c_float()
         check(self._lib.gas_batch_last_ms(self._h, C.byref(ms)), "gas_batch_last_ms")
         return float(ms.value)
+
+
+class GASServer:
+    """Serving loop over resident graphs (gas_server_*): submit BFS / SSSP /
+    PPR queries from any thread, wait for their results.
+
+    Results: int32 BFS depth / SSSP distance, float32 PPR rank, one value
+    per vertex.
+    """
+
+    def __init__(self, device: int = 0, lanes: int = 4, max_batch: int = 256,
+                 reserve_bytes: int = 1 << 30):
+        from ._lib import ServerConfig
+        self._lib = load()
+        cfg = ServerConfig(lanes, max_batch, reserve_bytes)
+        h = C.c_void_p()
+        check(self._lib.gas_server_create(device, C.byref(cfg), C.byref(h)), "gas_server_create")
+        self._h = h
+        self.n_vertices: dict[int, int] = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.gas_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_graph(self, n_vertices: int, srcs, dsts, weights=None) -> int:
+        s = np.ascontiguousarray(srcs, dtype=np.int32)
+        d = np.ascontiguousarray(dsts, dtype=np.int32)
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.int32)
+        gid = C.c_int32()
+        check(self._lib.gas_server_add_graph(self._h, n_vertices, int(s.shape[0]), _i32ptr(s),
+                                             _i32ptr(d), _i32ptr(w) if w is not None else None,
+                                             C.byref(gid)), "gas_server_add_graph")
+        self.n_vertices[gid.value] = n_vertices
+        return gid.value
+
+    def submit(self, graph: int, program: int, source: int) -> int:
+        t = C.c_uint64()
+        check(self._lib.gas_server_submit(self._h, graph, program, source, C.byref(t)),
+              "gas_server_submit")
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int32()
+        check(self._lib.gas_server_poll(self._h, ticket, C.byref(d)), "gas_server_poll")
+        return bool(d.value)
+
+    def wait(self, ticket: int, graph: int | None = None, program: int | None = None,
+             timeout_ms: int = -1, out: np.ndarray | None = None, want_result: bool = True):
+        """Returns (result array or None, info dict).  `out` may be a
+        preallocated (pinned) array of the graph's vertex count."""
+        from ._lib import PROGRAM_PPR, QueryInfo
+        info = QueryInfo()
+        res = out
+        if res is None and want_result:
+            if graph is None or program is None:
+                raise ValueError("graph and program are needed to size the result")
+            res = np.empty(self.n_vertices[graph],
+                           dtype=np.float32 if program == PROGRAM_PPR else np.int32)
+        ptr = res.ctypes.data_as(C.c_void_p) if res is not None else None
+        nbytes = res.nbytes if res is not None else 0
+        check(self._lib.gas_server_wait(self._h, ticket, timeout_ms, ptr, nbytes, C.byref(info)),
+              "gas_server_wait")
+        d = {f: getattr(info, f) for f, _ in QueryInfo._fields_ if f != "pad"}
+        return res, d
+
+    def stats(self) -> dict:
+        from ._lib import ServerStats
+        st = ServerStats()
+        check(self._lib.gas_server_get_stats(self._h, C.byref(st)), "gas_server_get_stats")
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
