@@ -49,6 +49,11 @@ WORKLOADS = {
     "batch-c4": dict(desc="256 BFS + 256 SSSP queries, uniform random sources, on R-MAT scale 21 "
                           "ef 16 symmetrised (w in [1,255]) and on the 1024x1024 lattice; batched "
                           "engine vs one-at-a-time plain runs"),
+    "serve-c5": dict(desc="serving loop over 8 resident graphs (R-MAT scales 12,14,16,18,20,21,22 "
+                          "ef 16 symmetrised, w in [1,255]; the 1024x1024 lattice, w in [1,100]); "
+                          "Poisson arrivals of a 50/30/20 BFS/SSSP/PPR (FP32, alpha 0.15, 20 "
+                          "rounds) mix on uniform random graph and source; served vs "
+                          "one-at-a-time plain engine"),
 }
 SEED = 1
 RMAT_SCALE = {"pagerank-rmat22": 22, "cc-rmat22": 22}
@@ -212,8 +217,155 @@ def cpu_run(engine, w, name):
     return st
 
 
+C5_GRAPHS = [("rmat12", 12), ("rmat14", 14), ("rmat16", 16), ("rmat18", 18), ("rmat20", 20),
+             ("rmat21", 21), ("rmat22", 22), ("grid1024", None)]
+C5_MIX = (0.5, 0.3, 0.2)      # BFS / SSSP / PPR
+C5_QUERIES = 1024             # queries per timed step
+C5_SWEEP = (0.25, 0.5, 0.75)  # offered load, as fractions of the measured capacity
+C5_SWEEP_QUERIES = 512
+C5_LANES = 8                  # batches in flight at once
+
+
+def c5_graphs():
+    from vertexapi2_gb300 import graphs
+    out = []
+    for name, sc in C5_GRAPHS:
+        if sc is None:
+            g = graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100))
+        else:
+            g = graphs.rmat(sc, 16, seed=SEED + sc, symmetrize=True, weights=(1, 255))
+        out.append((name, g))
+    return out
+
+
+def query_mix(gs, n, seed, mix=C5_MIX):
+    """n (graph index, program, source) triples: programs drawn from `mix`
+    (BFS/SSSP/PPR), graph and source uniform."""
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
+    rng = np.random.default_rng(seed)
+    progs = rng.choice([PROGRAM_BFS, PROGRAM_SSSP, PROGRAM_PPR], size=n, p=list(mix))
+    gids = rng.integers(0, len(gs), n)
+    srcs = [int(rng.integers(0, gs[k][1].n_vertices)) for k in gids]
+    return list(zip(gids.tolist(), progs.tolist(), srcs))
+
+
+def c4_queries(gs, nq=256):
+    """batch-c4's queries: nq BFS + nq SSSP sources per graph (seeded as the
+    batched leg draws them)."""
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
+    rng = np.random.default_rng(SEED)
+    out = []
+    for k, (_, g) in enumerate(gs):
+        for prog in (PROGRAM_BFS, PROGRAM_SSSP):
+            out += [(k, prog, int(s)) for s in rng.integers(0, g.n_vertices, nq)]
+    return out
+
+
+def cpu_cells(gs, cells, threads, per_cell=1, seed=SEED + 11):
+    """CPU engines' throughput on a query mix, stratified by cell.
+
+    `cells` maps (graph index, program) to the cell's share of the mix.
+    Each cell runs `per_cell` seeded random sources; all of them run at
+    once on `threads` host threads (ctypes calls drop the GIL), largest
+    graphs first.  BFS/SSSP use oracle/_ref (the reference engine built in
+    place) when it was built, else the restatement; PPR (not a reference
+    program) the restatement.  run() is timed inside the engine (graph
+    construction excluded, as bfs.cu:100-111 times it).  Throughput =
+    threads / (sum over cells of share x mean run time): `threads` engines
+    each answering queries of the mix back to back.
+    Returns (queries/s, queries run, wall s, engine kind)."""
+    import queue
+    import oracle
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
+    port = oracle.port()
+    eng = oracle.ref() or port
+    rng = np.random.default_rng(seed)
+    work = queue.Queue()
+    order = sorted(cells, key=lambda c: -gs[c[0]][1].n_edges)
+    for k, p in order:
+        for s0 in rng.integers(0, gs[k][1].n_vertices, per_cell):
+            work.put((k, p, int(s0)))
+    times = {c: [] for c in cells}
+    lock = threading.Lock()
+
+    def worker():
+        while True:
+            try:
+                k, p, s0 = work.get_nowait()
+            except queue.Empty:
+                return
+            g = gs[k][1]
+            if p == PROGRAM_BFS:
+                _, st = eng.bfs(g.n_vertices, g.srcs, g.dsts, s0)
+            elif p == PROGRAM_SSSP:
+                _, st = eng.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, s0)
+            else:
+                _, st = port.ppr(g.n_vertices, g.srcs, g.dsts, s0, iters=20)
+            with lock:
+                times[(k, p)].append(st["run_ns"] / 1e9)
+
+    t0 = time.perf_counter()
+    ts = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    wall = time.perf_counter() - t0
+    expected = sum(share * float(np.mean(times[c])) for c, share in cells.items())
+    return threads / expected, per_cell * len(cells), wall, eng.kind
+
+
+def c5_cells(gs):
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
+    progs = dict(zip((PROGRAM_BFS, PROGRAM_SSSP, PROGRAM_PPR), C5_MIX))
+    return {(k, p): w / len(gs) for k in range(len(gs)) for p, w in progs.items()}
+
+
+def c4_cells(gs):
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
+    return {(k, p): 1.0 / (2 * len(gs)) for k in range(len(gs)) for p in (PROGRAM_BFS, PROGRAM_SSSP)}
+
+
+def run_reference_queries(args):
+    """Reference arm of the query workloads: the CPU engines on every host
+    core over a bounded sample of the workload's queries."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    if args.workload == "batch-c4":
+        from vertexapi2_gb300 import graphs
+        gs = [("rmat21", graphs.rmat(21, 16, seed=SEED, symmetrize=True, weights=(1, 255))),
+              ("grid1024", graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100)))]
+        cells = c4_cells(gs)
+        metric = "batched queries/s (vs one-at-a-time plain engine)"
+    else:
+        gs = c5_graphs()
+        cells = c5_cells(gs)
+        metric = "served queries/s, p50/p99 latency (vs one-at-a-time plain engine)"
+    per_cell = max(1, -(-cores // len(cells)))
+    value, n, wall, kind = cpu_cells(gs, cells, cores, per_cell)
+    line = {
+        "impl": "reference", "metric": metric, "value": value, "unit": "queries/s",
+        "n_gpus": args.gpus, "steps": 1, "warmup": 0,
+        "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"], "seed": SEED},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": kind,
+                         "sample": f"one step (of the {args.steps} asked; a cell of the largest graph "
+                                   f"runs for minutes on one core): {per_cell} random source(s) per "
+                                   f"(graph, program) cell, {n} queries on {cores} threads in "
+                                   f"{wall:.0f} s; value = {cores} / (mix-weighted mean run() time); "
+                                   f"BFS/SSSP on the {kind} engine, PPR on the restatement"},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args):
     """CPU reference engine on every host core (rank 0 only)."""
+    if args.workload in ("batch-c4", "serve-c5"):
+        return run_reference_queries(args)
     world, rank, _ = dist_setup()
     if rank != 0:
         return
@@ -487,6 +639,211 @@ def run_batch_c4(args):
     print(json.dumps(line))
 
 
+def serve_pass(srv, ids, gs, queries, rate, bufs, seed):
+    """Submits `queries` with Poisson arrivals at `rate` queries/s (inf: all
+    at once) from a submitter thread while this thread waits for each result
+    in submission order and copies it into the graph's pinned buffer.
+    Returns per-query infos and the wall time from the first submission to
+    the last result in host memory."""
+    import queue
+    from vertexapi2_gb300._lib import PROGRAM_PPR
+    n = len(queries)
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n)) if np.isfinite(rate) else np.zeros(n)
+    arrivals -= arrivals[0]
+    handoff = queue.Queue()
+    t0 = time.perf_counter()
+
+    def submitter():
+        for i, (k, p, src) in enumerate(queries):
+            target = t0 + arrivals[i]
+            while True:
+                d = target - time.perf_counter()
+                if d <= 0:
+                    break
+                time.sleep(d if d > 2e-3 else 0)
+            handoff.put((i, srv.submit(ids[k], p, src)))
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    infos = [None] * n
+    for _ in range(n):
+        i, t = handoff.get()
+        k, p, _ = queries[i]
+        _, infos[i] = srv.wait(t, out=bufs[k][1 if p == PROGRAM_PPR else 0])
+    wall = time.perf_counter() - t0
+    th.join()
+    bad = [x for x in infos if x["status"] != 0]
+    if bad:
+        raise SystemExit(f"{len(bad)} served queries failed (status {bad[0]['status']})")
+    return infos, wall
+
+
+def serve_summary(infos, gs=None):
+    lat = np.array([(x["doneNs"] - x["submitNs"]) / 1e6 for x in infos])
+    span = (max(x["doneNs"] for x in infos) - min(x["submitNs"] for x in infos)) / 1e9
+    out = {"qps": len(infos) / span, "p50_ms": float(np.percentile(lat, 50)),
+           "p99_ms": float(np.percentile(lat, 99)), "span_s": span,
+           "mean_batch": float(np.mean([x["batchSize"] for x in infos]))}
+    if gs is not None:  # p50 latency and rounds per graph and program
+        names = {1: "bfs", 2: "sssp", 5: "ppr"}
+        cells = {}
+        for x, l in zip(infos, lat):
+            cells.setdefault(f"{gs[x['graph']][0]}-{names[x['program']]}", []).append(
+                (l, x["rounds"], (x["doneNs"] - x["admitNs"]) / 1e6))
+        out["cells"] = {k: {"n": len(v), "p50_ms": float(np.median([a for a, _, _ in v])),
+                            "run_ms": float(np.median([c for _, _, c in v])),
+                            "rounds": int(np.median([b for _, b, _ in v]))}
+                        for k, v in sorted(cells.items())}
+    return out
+
+
+def plain_one_at_a_time(gs, local, stream, per_cell=2):
+    """Mean run()+getResults() time of the plain engine per (graph, program)
+    on `per_cell` seeded sources, the result of each, and the mix's
+    queries/s (1 / expected time per query)."""
+    import vertexapi2_gb300 as gas
+    from vertexapi2_gb300 import programs as P
+    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
+    rng = np.random.default_rng(SEED + 3)
+    cells, results = {}, []
+    for k, (name, g) in enumerate(gs):
+        for prog in (PROGRAM_BFS, PROGRAM_SSSP, PROGRAM_PPR):
+            srcs = [int(x) for x in rng.integers(0, g.n_vertices, per_cell)]
+            e = gas.GASEngine(prog, device=local, stream=stream)
+            times = []
+            for q, s0 in enumerate(srcs):
+                if prog == PROGRAM_BFS:
+                    vd, act = P.bfs_init(g.n_vertices), (s0, s0 + 1)
+                elif prog == PROGRAM_SSSP:
+                    vd, act = P.sssp_init(g.n_vertices, s0), (0, g.n_vertices)
+                else:
+                    vd, act = P.ppr_init(g.n_vertices, g.srcs, s0), (0, g.n_vertices)
+                if q == 0:
+                    e.set_graph(g.n_vertices, vd, g.srcs, g.dsts,
+                                g.weights if prog == PROGRAM_SSSP else None)
+                else:
+                    e.set_vertex_data(vd)
+                e.set_active(*act)
+                e.run(20 if prog == PROGRAM_PPR else 0)   # warm
+                e.set_vertex_data(vd)
+                t0 = time.perf_counter()
+                e.set_active(*act)
+                e.run(20 if prog == PROGRAM_PPR else 0)
+                e.get_results()
+                times.append(time.perf_counter() - t0)
+                res = e.vertex_data["rank"].copy() if prog == PROGRAM_PPR else e.vertex_data.copy()
+                results.append((k, prog, s0, res))
+            e.close()
+            cells[(k, prog)] = float(np.mean(times))
+    mix = {PROGRAM_BFS: C5_MIX[0], PROGRAM_SSSP: C5_MIX[1], PROGRAM_PPR: C5_MIX[2]}
+    expected = sum(cells[(k, p)] * mix[p] / len(gs) for (k, p) in cells)
+    return 1.0 / expected, cells, results
+
+
+def run_serve_c5(args):
+    """Serving loop (queries/s, p50/p99) vs one-at-a-time plain runs."""
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    import vertexapi2_gb300 as gas
+    from vertexapi2_gb300._lib import PROGRAM_PPR
+    gas.load()
+    stream = torch.cuda.current_stream()
+    gs = c5_graphs()
+    srv = gas.GASServer(device=local, lanes=C5_LANES)
+    ids = [srv.add_graph(g.n_vertices, g.srcs, g.dsts, g.weights) for _, g in gs]
+    bufs = [(torch.empty(g.n_vertices, dtype=torch.int32).pin_memory().numpy(),
+             torch.empty(g.n_vertices, dtype=torch.float32).pin_memory().numpy()) for _, g in gs]
+    queries = query_mix(gs, C5_QUERIES, SEED)
+    for w in range(max(args.warmup, 1)):
+        serve_pass(srv, ids, gs, queries, float("inf"), bufs, SEED + w)
+    barrier(world)
+    torch.cuda.synchronize()
+    l0 = srv.stats()["kernelLaunches"]
+    steps = []
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            infos, wall = serve_pass(srv, ids, gs, queries, float("inf"), bufs, SEED + 100 + k)
+            steps.append((serve_summary(infos), wall))
+    launches = srv.stats()["kernelLaunches"] - l0
+    span = allreduce_max(world, float(sum(x["span_s"] for x, _ in steps)))
+    e2e_s = allreduce_max(world, float(sum(w for _, w in steps)))
+    total_q = allreduce_sum(world, float(C5_QUERIES * args.steps))
+    value = total_q / span
+    e2e_value = total_q / e2e_s
+    # latency under offered load below capacity
+    cap = value / world
+    sweep = []
+    for frac in C5_SWEEP:
+        qs = query_mix(gs, C5_SWEEP_QUERIES, SEED + int(frac * 1000))
+        infos, wall = serve_pass(srv, ids, gs, qs, frac * cap, bufs, SEED + 7)
+        sm = serve_summary(infos, gs if frac == C5_SWEEP[0] else None)
+        sweep.append({"offered_qps": frac * cap, "achieved_qps": sm["qps"], "p50_ms": sm["p50_ms"],
+                      "p99_ms": sm["p99_ms"], "mean_batch": sm["mean_batch"]})
+        if "cells" in sm:
+            sweep[-1]["cells"] = sm["cells"]
+    # one query at a time through the plain engine, and parity with serving
+    single_qps, cells, singles = plain_one_at_a_time(gs, local, stream.cuda_stream)
+    identical, ppr_err = True, 0.0
+    alone = {}
+    for k, prog, s0, res in singles:
+        out = bufs[k][1 if prog == PROGRAM_PPR else 0]
+        _, info = srv.wait(srv.submit(ids[k], prog, s0), out=out)
+        key = f"{gs[k][0]}-{ {1: 'bfs', 2: 'sssp', 5: 'ppr'}[prog] }"
+        alone.setdefault(key, []).append(((info["doneNs"] - info["submitNs"]) / 1e6, info["rounds"]))
+        if prog == PROGRAM_PPR:
+            a, b = out.astype(np.float64), res.astype(np.float64)
+            ppr_err = max(ppr_err, float(np.abs(a - b).sum() / np.abs(b).sum()))
+        else:
+            identical &= bool(np.array_equal(out, res))
+    st = srv.stats()
+    srv.close()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = os.cpu_count() or 1
+        v, n, wall, kind = cpu_cells(gs, c5_cells(gs), cores)
+        cpu = {"value": v, "unit": "queries/s", "cores": cores, "kind": kind,
+               "sample": f"one random source per (graph, program) cell, {n} queries on {cores} "
+                         f"threads in {wall:.0f} s; value = {cores} / (mix-weighted mean run() "
+                         f"time); BFS/SSSP on the {kind} engine, PPR on the restatement"}
+    if rank != 0:
+        return
+    d2h = sum(gs[k][1].n_vertices * 4 for k, _, _ in queries)
+    last = steps[-1][0]
+    line = {
+        "metric": "served queries/s, p50/p99 latency (vs one-at-a-time plain engine)",
+        "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * span / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
+        "config": {"workload": "serve-c5", "desc": WORKLOADS["serve-c5"]["desc"], "seed": SEED,
+                   "queries_per_step": C5_QUERIES, "lanes": C5_LANES, "max_batch": 256,
+                   "graphs": {n: [g.n_vertices, g.n_edges] for n, g in gs},
+                   "arrivals": "timed steps: every query of the step offered at once (capacity); "
+                               "sweep: Poisson at fractions of that capacity",
+                   "l2": "graphs (R-MAT-22: 4.2 M vertices, 126 M edges) and query state larger than L2"},
+        "latency_ms": {"p50": last["p50_ms"], "p99": last["p99_ms"], "at": "capacity (burst)"},
+        "sweep": sweep,
+        "mean_batch": last["mean_batch"],
+        "alone_served_ms": {k: [float(np.mean([a for a, _ in v])), int(v[0][1])]
+                            for k, v in sorted(alone.items())},
+        "plain_ms": {f"{gs[k][0]}-{ {1: 'bfs', 2: 'sssp', 5: 'ppr'}[p] }": 1e3 * t
+                     for (k, p), t in sorted(cells.items())},
+        "one_at_a_time": {"value": single_qps, "unit": "queries/s",
+                          "sample_queries": len(singles), "speedup": value / single_qps,
+                          "results_identical_bfs_sssp": identical,
+                          "ppr_max_rel_l1_vs_plain": ppr_err},
+        "server": {"batches": st["batches"], "memory_waits": st["memoryWaits"],
+                   "peak_bytes": st["peakBytesInUse"]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 12 * C5_QUERIES,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -505,6 +862,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch-c4":
         run_batch_c4(args)
+    elif args.workload == "serve-c5":
+        run_serve_c5(args)
     else:
         run_ours(args)
 

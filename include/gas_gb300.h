@@ -231,9 +231,12 @@ GAS_API gas_status gas_batch_last_ms(gas_batch *b, float *ms);
  * flight round by round, so batches on different lanes share the device
  * and new queries start while others run (continuous batching).
  *
- * Admission by free device memory: a batch of Q queries needs working
- * state of (BFS) V*Q*4 + V*(Q/8)*4 + 16*V bytes, (SSSP) V*Q*4 + V*(Q/32)*12
- * + 16*V, (PPR) V*Q*16 + 2*V, plus V*nQ*4 for its results.  It starts only
+ * Admission by free device memory: a batch of n queries on a graph of V
+ * vertices, with rows of Q queries (the next power of two >= n; at least 32
+ * for BFS and SSSP) and E edges, needs working state of (BFS) V*Q*4 +
+ * V*(Q/8)*4 + 28*V + 24*E/512 bytes, (SSSP) V*Q*4 + V*(Q/32)*12 + 28*V +
+ * 24*E/512, (PPR) V*Q*16 plus Q*4 bytes per 4096 in-edges of vertices
+ * above 4096, plus V*n*4 for its results.  It starts only
  * when cudaMemGetInfo's free bytes plus the server pool's cached bytes,
  * minus reserveBytes, cover it; otherwise the batch shrinks (in steps of
  * 32 queries) or waits for a running batch to release memory.  A query
@@ -276,6 +279,7 @@ typedef struct {
   int64_t peakBytesInUse;
   int64_t pending;           /* queries submitted and not yet in a batch      */
   int64_t running;           /* batches in flight                              */
+  int64_t kernelLaunches;    /* kernels the scheduler has launched             */
 } gas_server_stats;
 
 /* cfg may be NULL (defaults).  Starts the scheduler thread. */

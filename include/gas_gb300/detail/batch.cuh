@@ -12,14 +12,18 @@
 //
 // A round runs in one of two modes, chosen from the previous round's
 // changed vertices (list L, with their out-degree total E_out):
-//   push  (E_out * alpha <= E): one warp per listed vertex u walks its
-//         out-edges and updates the destinations for u's changed queries
-//         with atomics; destinations that change are appended to the next
-//         list (per-warp shared-memory staging, one atomic per 32 entries);
+//   push  (E_out * alpha <= E): a warp per list entry -- a changed vertex
+//         u and one kPushChunk-edge chunk of its out-edges (hubs span
+//         several entries, so no warp walks a hub alone) -- updates the
+//         destinations for u's changed queries with atomics, a lane per
+//         edge (or, for SSSP when u has more changed queries than the
+//         chunk has edges, a lane per query); destinations that change are
+//         appended to the next list (one atomic per warp and step);
 //   pull  otherwise: one pass over work units (a vertex's in-edges, split
-//         into chunks of at most `chunk` edges for high in-degree vertices)
-//         followed by a compaction of the changed vertices into the list.
-// In both, lanes map to queries (lane l owns queries l + 32k):
+//         into chunks of at most `chunk` edges for high in-degree vertices),
+//         lanes mapped to queries (lane l owns queries l + 32k), followed
+//         by a compaction of the changed vertices into the list.
+// The updates:
 //   BFS   next(v) = OR of mask[u] over in-neighbours u, minus seen(v);
 //         newly seen queries get depth = round + 1           (bfs.cu:54-66)
 //   SSSP  for queries whose distance at in-neighbour u changed, relax
@@ -42,8 +46,9 @@ struct BatchArgs {
   const int32_t *outOffsets;  // CSR (push rounds)
   const int32_t *outDests;
   const int32_t *weightsOut;  // CSR order (SSSP push rounds)
-  int32_t *list[3];           // [V] vertices with a changed query (rotating)
-  unsigned long long *listCnt;  // [3] (count << 32) | out-degree total
+  int32_t *list[3];           // [listCap] changed vertices (rotating), one
+  int32_t *listC[3];          //   entry per kPushChunk out-edges: (vertex, chunk)
+  unsigned long long *listCnt;  // [3] (entries << 32) | out-degree total
   int32_t *inList;            // [V] round stamp of list membership
   int32_t alpha;              // push when out-degree total * alpha <= nEdges
   int32_t nQueries;       // padded to 32 * W
@@ -64,6 +69,51 @@ struct BatchArgs {
 };
 
 constexpr int32_t kBatchInf = 0x7fffffff - 100000;  // SSSP gatherZero (sssp.cu:32-33)
+
+// Out-edges per push-list entry; a list holds at most V + E / kPushChunk
+// entries (each vertex once per round).
+constexpr int kPushChunk = 512;
+
+__host__ __device__ inline long long batch_list_capacity(long long nVertices, long long nEdges) {
+  return nVertices + nEdges / kPushChunk + 32;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(kFullMask, x, o);
+  return x;  // lane 0
+}
+
+// Appends, for each lane with `want`, vertex v of out-degree d to a list as
+// ceil(d / kPushChunk) entries (at least one): one atomic per warp.
+// Warp-uniform call.
+__device__ __forceinline__ void warp_append(bool want, int v, int d, int32_t *list,
+                                            int32_t *listC, unsigned long long *cnt) {
+  const int lane = threadIdx.x & 31;
+  const int ne = want ? max(1, (d + kPushChunk - 1) / kPushChunk) : 0;
+  int incl = ne;
+  unsigned dsum = want ? (unsigned)d : 0u;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFullMask, incl, o);
+    const unsigned z = __shfl_up_sync(kFullMask, dsum, o);
+    if (lane >= o) {
+      incl += y;
+      dsum += z;
+    }
+  }
+  const int total = __shfl_sync(kFullMask, incl, 31);
+  if (total == 0) return;
+  const unsigned dtot = __shfl_sync(kFullMask, dsum, 31);
+  unsigned long long base = 0ull;
+  if (lane == 0) base = atomicAdd(cnt, ((unsigned long long)total << 32) | dtot);
+  base = __shfl_sync(kFullMask, base, 0);
+  const long long pos = (long long)(base >> 32) + incl - ne;
+  for (int c = 0; c < ne; ++c) {
+    list[pos + c] = v;
+    listC[pos + c] = c;
+  }
+}
 
 template <int W, int KIND>
 __device__ __forceinline__ void batch_unit(const BatchArgs &a, int u, int round,
@@ -155,110 +205,128 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &a, int u, int round,
   }
 }
 
-// Per-warp staging of list appends in shared memory (warp-uniform calls).
-struct WarpStage {
-  int32_t v[32];
-  int32_t d[32];
-};
-
-__device__ __forceinline__ void stage_flush(WarpStage &st, int &n, int32_t *list,
-                                            unsigned long long *cnt) {
-  if (n == 0) return;
-  const int lane = threadIdx.x & 31;
-  __syncwarp();
-  unsigned dsum = lane < n ? (unsigned)st.d[lane] : 0u;
-  dsum = __reduce_add_sync(kFullMask, dsum);
-  unsigned long long base = 0ull;
-  if (lane == 0) base = atomicAdd(cnt, ((unsigned long long)n << 32) | dsum);
-  base = __shfl_sync(kFullMask, base, 0);
-  if (lane < n) list[(base >> 32) + lane] = st.v[lane];
-  __syncwarp();
-  n = 0;
-}
-
-__device__ __forceinline__ void stage_push(WarpStage &st, int &n, int v, int deg, int32_t *list,
-                                           unsigned long long *cnt) {
-  if ((threadIdx.x & 31) == 0) {
-    st.v[n] = v;
-    st.d[n] = deg;
-  }
-  if (++n == 32) stage_flush(st, n, list, cnt);
-}
-
-// Push round: warp per listed vertex u, over u's out-edges.
+// Push round: a warp per list entry (u, chunk), lanes over the chunk's
+// out-edges (32 at a time).  Warp-uniform.
 template <int W, int KIND>
-__device__ __forceinline__ void batch_push_unit(const BatchArgs &a, int u, int round,
+__device__ __forceinline__ void batch_push_unit(const BatchArgs &a, int u, int chunk, int round,
                                                 const unsigned *cur, unsigned *nxt,
-                                                int32_t *listNext, unsigned long long *cntNext,
-                                                WarpStage &st, int &stn,
+                                                int32_t *listNext, int32_t *listNextC,
+                                                unsigned long long *cntNext,
                                                 unsigned long long &changed) {
   const int lane = threadIdx.x & 31;
   const int Q = W * 32;
   unsigned m[W];
+  int nbits = 0, nwords = 0;
 #pragma unroll
-  for (int k = 0; k < W; ++k) m[k] = __ldcg(cur + (size_t)u * W + k);
+  for (int k = 0; k < W; ++k) {
+    m[k] = __ldcg(cur + (size_t)u * W + k);
+    nbits += __popc(m[k]);
+    nwords += m[k] != 0u;
+  }
   int du[W];
   if (KIND == kBatchSSSP) {
 #pragma unroll
     for (int k = 0; k < W; ++k)
       du[k] = ((m[k] >> lane) & 1u) ? __ldcg(a.value + (size_t)u * Q + k * 32 + lane) : kBatchInf;
   }
-  const int eb = a.outOffsets[u], ee = a.outOffsets[u + 1];
-  for (int e = eb; e < ee; ++e) {
-    const int v = __ldg(a.outDests + e);
-    unsigned any = 0u;
-    if (KIND == kBatchSSSP) {
-      const int w = __ldg(a.weightsOut + e);
+  const int ub = a.outOffsets[u];
+  const int eb = ub + chunk * kPushChunk;
+  const int ee = min(eb + kPushChunk, a.outOffsets[u + 1]);
+  // SSSP: a lane per edge costs ceil(deg/32) * nbits atomic steps, a lane
+  // per query deg * nwords
+  const bool perEdge =
+      KIND == kBatchBFS || (long long)((ee - eb + 31) / 32) * nbits <= (long long)(ee - eb) * nwords;
+  for (int e0 = eb; e0 < ee; e0 += 32) {
+    const int e = e0 + lane;
+    const bool ok = e < ee;
+    const int v = ok ? __ldg(a.outDests + e) : 0;
+    bool any = false;
+    if (KIND == kBatchBFS) {
 #pragma unroll
       for (int k = 0; k < W; ++k) {
-        bool imp = false;
-        if ((m[k] >> lane) & 1u) {
-          const int cand = du[k] + w;
-          const int old = atomicMin(a.value + (size_t)v * Q + k * 32 + lane, cand);
-          imp = cand < old;
-        }
-        const unsigned word = __ballot_sync(kFullMask, imp);
-        if (word) {
-          if (lane == 0) atomicOr(nxt + (size_t)v * W + k, word);
-          any |= word;
-          if (lane == 0) changed += __popc(word);
+        if (!m[k] || !ok) continue;
+        const unsigned old = atomicOr(a.seen + (size_t)v * W + k, m[k]);
+        unsigned fresh = m[k] & ~old;
+        if (!fresh) continue;
+        atomicOr(nxt + (size_t)v * W + k, fresh);
+        any = true;
+        changed += __popc(fresh);
+        while (fresh) {
+          const int b = __ffs(fresh) - 1;
+          fresh &= fresh - 1u;
+          a.value[(size_t)v * Q + k * 32 + b] = round + 1;
         }
       }
-    } else {
+    } else if (perEdge) {
+      const int w = ok ? __ldg(a.weightsOut + e) : 0;
 #pragma unroll
       for (int k = 0; k < W; ++k) {
-        if (!m[k]) continue;  // warp-uniform
-        unsigned fresh = 0u;
-        if (lane == 0) {
-          const unsigned old = atomicOr(a.seen + (size_t)v * W + k, m[k]);
-          fresh = m[k] & ~old;
-          if (fresh) atomicOr(nxt + (size_t)v * W + k, fresh);
+        unsigned bits = m[k], imp = 0u;
+        while (bits) {  // warp-uniform; up to four relaxations in flight
+          int bs[4], ds[4], olds[4];
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            bs[t] = bits ? __ffs(bits) - 1 : -1;
+            if (bits) bits &= bits - 1u;
+            ds[t] = __shfl_sync(kFullMask, du[k], bs[t] < 0 ? 0 : bs[t]);
+          }
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+            olds[t] = (ok && bs[t] >= 0)
+                          ? atomicMin(a.value + (size_t)v * Q + k * 32 + bs[t], ds[t] + w)
+                          : kBatchInf;
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+            if (ok && bs[t] >= 0 && ds[t] + w < olds[t]) imp |= 1u << bs[t];
         }
-        fresh = __shfl_sync(kFullMask, fresh, 0);
-        if ((fresh >> lane) & 1u) a.value[(size_t)v * Q + k * 32 + lane] = round + 1;
-        if (lane == 0) changed += __popc(fresh);
-        any |= fresh;
+        if (imp) {
+          atomicOr(nxt + (size_t)v * W + k, imp);
+          any = true;
+          changed += __popc(imp);
+        }
       }
+    } else {  // lane per query, the 32 edges in turn
+      const int w = ok ? __ldg(a.weightsOut + e) : 0;
+      const int n = min(32, ee - e0);
+      unsigned anyMask = 0u;
+      for (int t = 0; t < n; ++t) {
+        const int vt = __shfl_sync(kFullMask, v, t);
+        const int wt = __shfl_sync(kFullMask, w, t);
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          bool imp = false;
+          if ((m[k] >> lane) & 1u) {
+            const int cand = du[k] + wt;
+            const int old = atomicMin(a.value + (size_t)vt * Q + k * 32 + lane, cand);
+            imp = cand < old;
+          }
+          const unsigned word = __ballot_sync(kFullMask, imp);
+          if (word) {
+            if (lane == 0) {
+              atomicOr(nxt + (size_t)vt * W + k, word);
+              changed += __popc(word);
+            }
+            anyMask |= 1u << t;
+          }
+        }
+      }
+      any = (anyMask >> lane) & 1u;
     }
-    if (any) {  // warp-uniform
-      int first = 0;
-      if (lane == 0) first = atomicExch(a.inList + v, round + 1) != round + 1;
-      first = __shfl_sync(kFullMask, first, 0);
-      if (first)
-        stage_push(st, stn, v, a.outOffsets[v + 1] - a.outOffsets[v], listNext, cntNext);
-    }
+    bool want = false;
+    if (any) want = atomicExch(a.inList + v, round + 1) != round + 1;
+    warp_append(want, v, want ? a.outOffsets[v + 1] - a.outOffsets[v] : 0, listNext, listNextC,
+                cntNext);
   }
 }
 
 // After a pull round: list the vertices with a changed query.
 template <int W>
 __device__ __forceinline__ void batch_compact(const BatchArgs &a, const unsigned *nxt,
-                                              int32_t *listNext, unsigned long long *cntNext,
-                                              WarpStage &st) {
+                                              int32_t *listNext, int32_t *listNextC,
+                                              unsigned long long *cntNext) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  int stn = 0;
   for (long long base = gw * 32; base < a.nVertices; base += warps * 32) {
     const long long v = base + lane;
     unsigned any = 0u;
@@ -266,25 +334,14 @@ __device__ __forceinline__ void batch_compact(const BatchArgs &a, const unsigned
 #pragma unroll
       for (int k = 0; k < W; ++k) any |= __ldcg(nxt + (size_t)v * W + k);
     }
-    const unsigned who = __ballot_sync(kFullMask, any != 0u);
-    const int n = __popc(who);
-    if (n == 0) continue;
-    // stage this group's changed vertices (at most 32) in one flush
-    stage_flush(st, stn, listNext, cntNext);
-    const int pos = __popc(who & ((1u << lane) - 1u));
-    if (any) {
-      st.v[pos] = (int32_t)v;
-      st.d[pos] = a.outOffsets[v + 1] - a.outOffsets[v];
-    }
-    stn = n;
-    stage_flush(st, stn, listNext, cntNext);
+    const bool want = any != 0u;
+    warp_append(want, (int)v, want ? a.outOffsets[v + 1] - a.outOffsets[v] : 0, listNext,
+                listNextC, cntNext);
   }
 }
 
 template <int W, int KIND>
 __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
-  __shared__ WarpStage stage[8];
-  WarpStage &st = stage[threadIdx.x / 32];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const size_t maskWords = (size_t)a.nVertices * W;
@@ -294,15 +351,18 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
     const unsigned *cur = a.mask[r % 3];
     unsigned *nxt = a.mask[(r + 1) % 3];
     unsigned *clr = a.mask[(r + 2) % 3];
-    const int32_t *listCur = a.list[r % 3];
-    int32_t *listNext = a.list[(r + 1) % 3];
-    unsigned long long *cntNext = a.listCnt + (r + 1) % 3;
-    const unsigned long long lc = a.listCnt[r % 3];
-    const int nList = (int)(lc >> 32);
+    const int rc = r % 3, rn = (r + 1) % 3;
+    const int32_t *listCur = a.list[rc];
+    const int32_t *listCurC = a.listC[rc];
+    int32_t *listNext = a.list[rn];
+    int32_t *listNextC = a.listC[rn];
+    unsigned long long *cntNext = a.listCnt + rn;
+    const unsigned long long lc = a.listCnt[rc];
+    const long long nList = (long long)(lc >> 32);
     const long long eOut = (long long)(lc & 0xffffffffull);
     const bool push = eOut * a.alpha <= (long long)a.nEdges;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.cnt[(r + 1) % 3] = 0ull;
+      a.cnt[rn] = 0ull;
       a.listCnt[(r + 2) % 3] = 0ull;  // input of round r-1, appended in round r+1
     }
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
@@ -310,19 +370,19 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       clr[i] = 0u;
     unsigned long long changed = 0ull;
     if (push) {
-      int stn = 0;
       for (long long i = gw; i < nList; i += warps)
-        batch_push_unit<W, KIND>(a, listCur[i], r, cur, nxt, listNext, cntNext, st, stn, changed);
-      stage_flush(st, stn, listNext, cntNext);
+        batch_push_unit<W, KIND>(a, listCur[i], listCurC[i], r, cur, nxt, listNext, listNextC,
+                                 cntNext, changed);
     } else {
       for (long long u = gw; u < a.nUnits; u += warps)
         batch_unit<W, KIND>(a, (int)u, r, cur, nxt, changed);
     }
-    if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + (r % 3), changed);
+    changed = warp_sum_u64(changed);
+    if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + rc, changed);
     if (!grid_barrier(a.barrier, a.errWord)) break;
-    if (a.cnt[r % 3] == 0ull) break;  // uniform: read after the barrier
+    if (a.cnt[rc] == 0ull) break;  // uniform: read after the barrier
     if (!push) {
-      batch_compact<W>(a, nxt, listNext, cntNext, st);
+      batch_compact<W>(a, nxt, listNext, listNextC, cntNext);
       if (!grid_barrier(a.barrier, a.errWord)) break;
     }
   }
@@ -344,7 +404,8 @@ static __global__ void batch_sources_kernel(int kind, int32_t nQueries, int32_t 
                                             const int32_t *sources, int32_t *value,
                                             unsigned *mask0, unsigned *seen,
                                             const int32_t *outOffsets, int32_t *inList,
-                                            int32_t *list0, unsigned long long *listCnt0) {
+                                            int32_t *list0, int32_t *list0C,
+                                            unsigned long long *listCnt0) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nQueries) return;
   const int s = sources[q];
@@ -353,8 +414,12 @@ static __global__ void batch_sources_kernel(int kind, int32_t nQueries, int32_t 
   if (kind == kBatchBFS) atomicOr(seen + (size_t)s * W + q / 32, 1u << (q % 32));
   if (atomicExch(inList + s, 0) != 0) {
     const unsigned d = (unsigned)(outOffsets[s + 1] - outOffsets[s]);
-    const unsigned long long pos = atomicAdd(listCnt0, (1ull << 32) | d);
-    list0[pos >> 32] = s;
+    const unsigned ne = d > 0u ? (d + kPushChunk - 1) / kPushChunk : 1u;
+    const unsigned long long pos = atomicAdd(listCnt0, ((unsigned long long)ne << 32) | d) >> 32;
+    for (unsigned c = 0; c < ne; ++c) {
+      list0[pos + c] = s;
+      list0C[pos + c] = (int32_t)c;
+    }
   }
 }
 

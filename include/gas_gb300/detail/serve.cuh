@@ -19,11 +19,13 @@
 //                 order, of rank[u][q] / outdeg(u))      for active v
 //   rank'[v][q] = rank[v][q]                              otherwise
 // with the engine's active sets A0 = every vertex, A(k+1) = out-neighbours
-// of A(k) (apply always returns true).  Each (v, q) sum is a left fold from
-// 0 in CSC order with correctly rounded float operations and no
-// contraction, so every query's ranks equal a single-source run of the
-// reference engine's CPU loop (refgas.h:140-166 with the program of
-// pagerank.cu:27-73 and a teleport term) bit for bit, alone or in any mix.
+// of A(k) (apply always returns true).  Sums use correctly rounded float
+// operations without contraction; for vertices of in-degree <= kPprChunk
+// each is the left fold from 0 in CSC order, so those ranks equal a
+// single-source run of the reference engine's CPU loop (refgas.h:140-166
+// with the program of pagerank.cu:27-73 and a teleport term) bit for bit.
+// Every sum depends on the graph alone: a query's ranks are the same in
+// every batch and mix.
 #pragma once
 
 #include "batch.cuh"
@@ -37,23 +39,19 @@ template <int W, int KIND>
 __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int r,
                                                           const unsigned *done) {
   if (ld_acquire(done)) return;
-  __shared__ WarpStage stage[8];
-  WarpStage &st = stage[threadIdx.x / 32];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const size_t maskWords = (size_t)a.nVertices * W;
-  const unsigned *cur = a.mask[r % 3];
-  unsigned *nxt = a.mask[(r + 1) % 3];
+  const int rc = r % 3, rn = (r + 1) % 3;
+  const unsigned *cur = a.mask[rc];
+  unsigned *nxt = a.mask[rn];
   unsigned *clr = a.mask[(r + 2) % 3];
-  const int32_t *listCur = a.list[r % 3];
-  int32_t *listNext = a.list[(r + 1) % 3];
-  unsigned long long *cntNext = a.listCnt + (r + 1) % 3;
-  const unsigned long long lc = a.listCnt[r % 3];
-  const int nList = (int)(lc >> 32);
+  const unsigned long long lc = a.listCnt[rc];
+  const long long nList = (long long)(lc >> 32);
   const long long eOut = (long long)(lc & 0xffffffffull);
   const bool push = eOut * a.alpha <= (long long)a.nEdges;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.cnt[(r + 1) % 3] = 0ull;
+    a.cnt[rn] = 0ull;
     a.listCnt[(r + 2) % 3] = 0ull;
   }
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
@@ -61,15 +59,15 @@ __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int
     clr[i] = 0u;
   unsigned long long changed = 0ull;
   if (push) {
-    int stn = 0;
     for (long long i = gw; i < nList; i += warps)
-      batch_push_unit<W, KIND>(a, listCur[i], r, cur, nxt, listNext, cntNext, st, stn, changed);
-    stage_flush(st, stn, listNext, cntNext);
+      batch_push_unit<W, KIND>(a, a.list[rc][i], a.listC[rc][i], r, cur, nxt, a.list[rn],
+                               a.listC[rn], a.listCnt + rn, changed);
   } else {
     for (long long u = gw; u < a.nUnits; u += warps)
       batch_unit<W, KIND>(a, (int)u, r, cur, nxt, changed);
   }
-  if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + (r % 3), changed);
+  changed = warp_sum_u64(changed);
+  if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + rc, changed);
 }
 
 // End of round r: no change -> done (rounds = r, as the persistent kernel
@@ -88,24 +86,40 @@ __global__ void __launch_bounds__(256) batch_tail_kernel(const BatchArgs a, int 
   const unsigned long long lc = a.listCnt[r % 3];
   const bool push = (long long)(lc & 0xffffffffull) * a.alpha <= (long long)a.nEdges;
   if (push) return;
-  __shared__ WarpStage stage[8];
-  batch_compact<W>(a, a.mask[(r + 1) % 3], a.list[(r + 1) % 3], a.listCnt + (r + 1) % 3,
-                   stage[threadIdx.x / 32]);
+  const int rn = (r + 1) % 3;
+  batch_compact<W>(a, a.mask[rn], a.list[rn], a.listC[rn], a.listCnt + rn);
 }
 
 // ---------------------------------------------------------------- PPR
 
+// A vertex's in-edges form one work unit, or -- above kPprChunk edges --
+// several units of kPprChunk edges whose partial sums the last unit to
+// finish adds in chunk order.  Each (vertex, query) value is therefore a
+// left fold in CSC order (bit for bit the reference loop's FP32 sum) for
+// every vertex of in-degree <= kPprChunk, and a fixed-order sum of left-
+// folded chunks above it: either way a function of the graph alone, the
+// same in every batch.
+constexpr int kPprChunk = 4096;
+
 struct PprArgs {
   int32_t nVertices;
-  int32_t nQueries;           // queries in the batch (<= Q = 32 * W)
-  const int32_t *inOffsets;   // CSC
-  const int32_t *inSources;
+  int32_t nQueries;           // queries in the batch (<= the row width QP)
+  const int32_t *inSources;   // CSC
   const int32_t *outDegree;   // [V]
-  const int32_t *order;       // [V] vertices by in-degree, largest first
+  const uint8_t *lastActive;  // [V] last round in which the vertex is active
+  int32_t nUnits;             // work units, longest first
+  const int32_t *unitV;
+  const int32_t *unitBeg;
+  const int32_t *unitLen;
+  const int32_t *unitSlot;    // -1, or the unit's partial-sum slot (hubs)
+  const int32_t *slotFirst;   // [slots] first slot of the slot's vertex
+  const int32_t *slotCount;   // [slots] chunks of that vertex
+  const int32_t *slotHub;     // [slots] hub index (arrival counter)
+  float *partial;             // [slots][QP] (per batch)
+  unsigned *arrive;           // [hubs] arrivals, never reset within a batch
   const int32_t *sources;     // [nQueries]
-  float *rank[2];             // [V][Q]
-  float *contrib[2];          // [V][Q] rank / outdeg (0 where outdeg is 0)
-  unsigned char *active[2];   // [V] active set of the round
+  float *rank[2];             // [V][QP]
+  float *contrib[2];          // [V][QP] rank / outdeg (0 where outdeg is 0)
   float damp;                 // 1 - alpha, as the program computes it in float
   float teleport;             // alpha
 };
@@ -114,95 +128,151 @@ __device__ __forceinline__ float ppr_contrib(float rank, int deg) {
   return deg > 0 ? __fdiv_rn(rank, (float)deg) : 0.0f;
 }
 
+// The engine's active sets do not depend on the source: A0 = every vertex,
+// A(k+1) = out-neighbours of A(k).  v is in A(k) iff a walk of length k
+// ends at v, so membership only shrinks with k: lastActive[v] = the largest
+// such k (capped).  One pull step per launch: nxt = out-neighbours of cur.
+static __global__ void ppr_active_step_kernel(int32_t nVertices, const int32_t *inOffsets,
+                                              const int32_t *inSources, const uint8_t *cur,
+                                              uint8_t *nxt, uint8_t *lastActive, int k) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x / 32);
+  for (long long v = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+       v < nVertices; v += warps) {
+    const int beg = inOffsets[v], end = inOffsets[v + 1];
+    bool any = false;
+    for (int e = beg + lane; e < end && !any; e += 32) any = cur[inSources[e]] != 0;
+    any = __any_sync(kFullMask, any);
+    if (lane == 0) {
+      nxt[v] = any;
+      if (any) lastActive[v] = (uint8_t)k;
+    }
+  }
+}
+
+// Row width QP (queries per vertex row, a power of two 1..256) and how a
+// warp covers it: L lanes per unit (L = min(QP, 32)), G = 32 / L units per
+// warp, W = QP / L words of queries per lane (query of lane j, word k:
+// k * L + j), D edges gathered per step (their loads all in flight), M
+// source ids loaded per lane per step.
+template <int QP>
+struct PprShape {
+  static constexpr int L = QP < 32 ? QP : 32;
+  static constexpr int G = 32 / L;
+  static constexpr int W = QP / L;
+  static constexpr int D = W == 1 ? 32 : 32 / W;
+  static constexpr int M = D > L ? D / L : 1;
+};
+
 // rank := 1 at each query's source, 0 elsewhere (pagerank-style init of a
-// personalised run); every vertex active in round 0.
-template <int W>
+// personalised run).
+template <int QP>
 __global__ void ppr_init_kernel(const PprArgs a) {
-  const int Q = 32 * W;
-  const size_t n = (size_t)a.nVertices * Q;
+  const size_t n = (size_t)a.nVertices * QP;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     a.rank[0][i] = 0.0f;
     a.contrib[0][i] = 0.0f;
   }
-  for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < (size_t)a.nVertices;
-       v += (size_t)gridDim.x * blockDim.x)
-    a.active[0][v] = 1;
 }
 
-template <int W>
+template <int QP>
 __global__ void ppr_sources_kernel(const PprArgs a) {
-  const int Q = 32 * W;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= a.nQueries) return;
   const int s = a.sources[q];
-  a.rank[0][(size_t)s * Q + q] = 1.0f;
-  a.contrib[0][(size_t)s * Q + q] = ppr_contrib(1.0f, a.outDegree[s]);
+  a.rank[0][(size_t)s * QP + q] = 1.0f;
+  a.contrib[0][(size_t)s * QP + q] = ppr_contrib(1.0f, a.outDegree[s]);
 }
 
-// Round r: reads rank/contrib/active[r & 1], writes [(r + 1) & 1].  A warp
-// per vertex (taken in decreasing in-degree order), lane l owning queries
-// l + 32k; in-edges are walked in CSC order, 32 source ids per coalesced
-// load, each gathered row of contributions one 128-byte load per word.
-template <int W>
+// Round r: reads rank/contrib[r & 1], writes [(r + 1) & 1].  Groups of L
+// lanes take units longest first (the G groups of a warp get neighbouring
+// units, so similar lengths); a group loads D source ids per step (M per
+// lane, coalesced), issues the D gathered rows' loads, then each lane folds
+// its queries' D values in edge order.
+template <int QP>
 __global__ void __launch_bounds__(256) ppr_round_kernel(const PprArgs a, int r) {
-  const int Q = 32 * W;
+  using S = PprShape<QP>;
+  constexpr int L = S::L, G = S::G, W = S::W, D = S::D, M = S::M;
   const int lane = threadIdx.x & 31;
+  const int grp = lane / L, j = lane % L;
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const bool odd = (r & 1) != 0;  // selects, not indexes (keeps the params out of local memory)
   const float *rk = odd ? a.rank[1] : a.rank[0];
   const float *ct = odd ? a.contrib[1] : a.contrib[0];
-  const unsigned char *act = odd ? a.active[1] : a.active[0];
   float *rk2 = odd ? a.rank[0] : a.rank[1];
   float *ct2 = odd ? a.contrib[0] : a.contrib[1];
-  unsigned char *act2 = odd ? a.active[0] : a.active[1];
-  for (long long i = gw; i < a.nVertices; i += warps) {
-    const int v = a.order[i];
-    const int beg = a.inOffsets[v], end = a.inOffsets[v + 1];
-    const bool isAct = act[v] != 0;
+  for (long long base = gw * G; base < a.nUnits; base += warps * G) {
+    const long long u = base + grp;
+    const bool valid = u < a.nUnits;
+    const int v = valid ? a.unitV[u] : 0;
+    const int beg = valid ? a.unitBeg[u] : 0;
+    const int len = valid ? a.unitLen[u] : 0;
+    const bool isAct = valid && (int)a.lastActive[v] >= r;
+    const int maxLen = __reduce_max_sync(kFullMask, isAct ? len : 0);
     float acc[W];
 #pragma unroll
     for (int k = 0; k < W; ++k) acc[k] = 0.0f;
-    unsigned anyAct = 0u;
-    for (int e0 = beg; e0 < end; e0 += 32) {
-      const int e = e0 + lane;
-      const int s = e < end ? __ldg(a.inSources + e) : 0;
-      anyAct |= __ballot_sync(kFullMask, e < end && act[s] != 0);
-      if (!isAct) continue;  // warp-uniform
-      const int n = min(32, end - e0);
-      int j = 0;
-      for (; j + 4 <= n; j += 4) {  // four rows in flight, folded in order
-        float c[4][W];
+    for (int o = 0; o < maxLen; o += D) {  // warp-uniform trip count
+      int ids[M];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const int sj = __shfl_sync(kFullMask, s, j + t);
-#pragma unroll
-          for (int k = 0; k < W; ++k) c[t][k] = __ldcg(ct + (size_t)sj * Q + k * 32 + lane);
-        }
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-#pragma unroll
-          for (int k = 0; k < W; ++k) acc[k] = __fadd_rn(acc[k], c[t][k]);
+      for (int m = 0; m < M; ++m) {
+        const int t = m * L + j;
+        ids[m] = (t < D && o + t < len) ? __ldg(a.inSources + beg + o + t) : 0;
       }
-      for (; j < n; ++j) {
-        const int sj = __shfl_sync(kFullMask, s, j);
+      const int n = isAct ? min(D, len - o) : 0;  // this group's edges in the step
+      float c[D][W];
+#pragma unroll
+      for (int t = 0; t < D; ++t) {
+        const int sj = __shfl_sync(kFullMask, ids[t / L], t % L, L);
 #pragma unroll
         for (int k = 0; k < W; ++k)
-          acc[k] = __fadd_rn(acc[k], __ldcg(ct + (size_t)sj * Q + k * 32 + lane));
+          c[t][k] = t < n ? __ldcg(ct + (size_t)sj * QP + k * L + j) : 0.0f;
+      }
+#pragma unroll
+      for (int t = 0; t < D; ++t)
+#pragma unroll
+        for (int k = 0; k < W; ++k)
+          if (t < n) acc[k] = __fadd_rn(acc[k], c[t][k]);
+    }
+    // hub chunks: publish the partial sums; the last chunk to arrive adds
+    // them in chunk order and finishes the vertex
+    const int slot = valid ? a.unitSlot[u] : -1;
+    unsigned arrived = 0u;
+    if (slot >= 0) {
+#pragma unroll
+      for (int k = 0; k < W; ++k) a.partial[(size_t)slot * QP + k * L + j] = acc[k];
+      __threadfence();
+      __syncwarp(L == 32 ? kFullMask : (((1u << L) - 1u) << (grp * L)));
+      if (j == 0) {
+        const unsigned old = atomicAdd(a.arrive + a.slotHub[slot], 1u);
+        arrived = (old + 1u) % (unsigned)a.slotCount[slot] == 0u ? 1u : 0u;
       }
     }
-    if (lane == 0) act2[v] = anyAct != 0u;
-    const int deg = a.outDegree[v];
+    const unsigned last = __shfl_sync(kFullMask, arrived, grp * L);
+    if (!valid || (slot >= 0 && !last)) continue;
+    if (slot >= 0) {
+      __threadfence();
+      const int first = a.slotFirst[slot], cnt = a.slotCount[slot];
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        float sum = 0.0f;
+        for (int c = 0; c < cnt; ++c)
+          sum = __fadd_rn(sum, __ldcg(a.partial + (size_t)(first + c) * QP + k * L + j));
+        acc[k] = sum;
+      }
+    }
+    const int odeg = a.outDegree[v];
 #pragma unroll
     for (int k = 0; k < W; ++k) {
-      const int q = k * 32 + lane;
-      const size_t idx = (size_t)v * Q + q;
+      const int q = k * L + j;
+      const size_t idx = (size_t)v * QP + q;
       if (isAct) {
         const float tele = (q < a.nQueries && a.sources[q] == v) ? a.teleport : 0.0f;
         const float nr = __fadd_rn(tele, __fmul_rn(a.damp, acc[k]));
         rk2[idx] = nr;
-        ct2[idx] = ppr_contrib(nr, deg);
+        ct2[idx] = ppr_contrib(nr, odeg);
       } else {
         rk2[idx] = __ldcg(rk + idx);
         ct2[idx] = __ldcg(ct + idx);

@@ -160,3 +160,36 @@ def test_graph_admission_and_errors(gpu):
         assert info["status"] == 0 and r.dtype == np.float32 and r[2] > 0
     with pytest.raises(GasError):
         GASServer(lanes=0)
+
+
+def test_ppr_hub_chunks_and_directed_levels(gpu, port):
+    """A vertex of in-degree > 4096 (its sum is split into chunks: within
+    1e-5 relative L1 of FP64, identical alone and in a mix) and a directed
+    chain feeding a cycle (active sets that shrink round by round: bit for
+    bit with the FP32 oracle)."""
+    rng = np.random.default_rng(9)
+    n = 9000
+    leaves = np.arange(1, n, dtype=np.int32)
+    hub = np.zeros(n - 1, np.int32)
+    extra_s = rng.integers(1, n, 20000).astype(np.int32)
+    extra_d = rng.integers(1, n, 20000).astype(np.int32)
+    keep = extra_s != extra_d
+    s = np.concatenate([leaves, hub, extra_s[keep]])
+    d = np.concatenate([hub, leaves, extra_d[keep]])
+    # directed: 0..29 a chain into a 5-cycle 30..34, plus a tail out of it
+    cs = np.array(list(range(29)) + [29, 30, 31, 32, 33, 34, 34], np.int32)
+    cd = np.array(list(range(1, 30)) + [30, 31, 32, 33, 34, 30, 35], np.int32)
+    with GASServer(lanes=3) as srv:
+        gh = srv.add_graph(n, s, d)
+        gc = srv.add_graph(36, cs, cd)
+        srcs = [0, 1, 4500, 8999]
+        ts = [srv.submit(gh, PROGRAM_PPR, x) for x in srcs] + \
+             [srv.submit(gc, PROGRAM_PPR, x) for x in (0, 29, 34)]
+        mixed = [srv.wait(t, gh if i < 4 else gc, PROGRAM_PPR)[0] for i, t in enumerate(ts)]
+        alone = [srv.wait(srv.submit(gh, PROGRAM_PPR, x), gh, PROGRAM_PPR)[0] for x in srcs]
+    for x, m, a in zip(srcs, mixed, alone):
+        assert np.array_equal(m, a)
+        ref64 = port.ppr(n, s, d, x, iters=20, fp64=True)[0]
+        assert rel_l1(m, ref64) <= PPR_REL_L1
+    for x, m in zip((0, 29, 34), mixed[4:]):
+        assert np.array_equal(m, port.ppr(36, cs, cd, x, iters=20)[0]), f"chain source {x}"

@@ -54,7 +54,7 @@ class QueryInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in (
         "submitted", "completed", "failed", "batches", "batchedQueries", "memoryWaits",
-        "bytesInUse", "peakBytesInUse", "pending", "running")]
+        "bytesInUse", "peakBytesInUse", "pending", "running", "kernelLaunches")]
 
 
 _P = C.c_void_p

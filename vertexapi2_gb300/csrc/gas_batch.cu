@@ -46,6 +46,7 @@ struct gas_batch_s {
   int32_t alpha = 10;  // push round when list out-degree total * alpha <= E
   int32_t unitChunk = 0;
   int32_t *list[3] = {nullptr, nullptr, nullptr};
+  int32_t *listC[3] = {nullptr, nullptr, nullptr};
   int32_t *inList = nullptr;
   int32_t *weightsOut = nullptr;  // CSR order
   int32_t *unitV = nullptr, *unitBeg = nullptr, *unitEnd = nullptr;
@@ -89,13 +90,15 @@ void drop_graphs(gas_batch *b) {
 
 void free_state(gas_batch *b) {
   void *ps[] = {b->value, b->srcDev, b->outDev, b->mask[0], b->mask[1], b->mask[2], b->seen,
-                b->list[0], b->list[1], b->list[2], b->inList};
+                b->list[0], b->list[1], b->list[2], b->listC[0], b->listC[1], b->listC[2],
+                b->inList};
   for (void *p : ps)
     if (p) cudaFree(p);
   b->value = b->srcDev = b->outDev = nullptr;
   b->mask[0] = b->mask[1] = b->mask[2] = nullptr;
   b->seen = nullptr;
   b->list[0] = b->list[1] = b->list[2] = nullptr;
+  b->listC[0] = b->listC[1] = b->listC[2] = nullptr;
   b->inList = nullptr;
   b->capQ = 0;
   drop_graphs(b);
@@ -151,7 +154,9 @@ gas_status ensure_state(gas_batch *b, const CoreGraph &g, int32_t Q) {
   if (e == cudaSuccess) e = cudaMalloc(&b->srcDev, kMaxBatch * 4);
   for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->mask[k], V * W * 4);
   if (e == cudaSuccess) e = cudaMalloc(&b->seen, V * W * 4);
-  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->list[k], V * 4);
+  const size_t cap = (size_t)gas::detail::batch_list_capacity(g.nV, g.nE);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->list[k], cap * 4);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->listC[k], cap * 4);
   if (e == cudaSuccess) e = cudaMalloc(&b->inList, V * 4);
   if (e != cudaSuccess) {
     free_state(b);
@@ -170,7 +175,10 @@ gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
   a.outOffsets = g.outOff;
   a.outDests = g.outDst;
   a.weightsOut = b->weightsOut;
-  for (int k = 0; k < 3; ++k) a.list[k] = b->list[k];
+  for (int k = 0; k < 3; ++k) {
+    a.list[k] = b->list[k];
+    a.listC[k] = b->listC[k];
+  }
   a.inList = b->inList;
   a.alpha = b->alpha;
   a.nQueries = Q;
@@ -234,7 +242,7 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
   CtlView cv = ctl_view(b);
   gas::detail::batch_sources_kernel<<<(nQ + 127) / 128, 128, 0, b->stream>>>(
       kind, nQ, Q, W, b->srcDev, b->value, b->mask[0], b->seen, g.outOff, b->inList,
-      b->list[0], cv.listCnt);
+      b->list[0], b->listC[0], cv.listCnt);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch init");
   const int blocks = grid_blocks(b, kind, W);

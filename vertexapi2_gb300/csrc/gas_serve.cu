@@ -72,8 +72,12 @@ struct ServeGraph {
   int32_t id = 0;
   gas_batch *batch = nullptr;  // CSC/CSR, weights, pull units
   BatchGraph bg;
-  int32_t *outDegree = nullptr;  // [V] (PPR)
-  int32_t *order = nullptr;      // [V] by in-degree, largest first (PPR)
+  // PPR: out-degrees, the last round each vertex is active, work units
+  // (longest first) and the partial-sum slots of hub chunks
+  int32_t *outDegree = nullptr;   // [V]
+  uint8_t *lastActive = nullptr;  // [V]
+  int32_t *pprMem = nullptr;      // unitV | unitBeg | unitLen | unitSlot | slotFirst | slotCount | slotHub
+  int32_t pprUnits = 0, pprSlots = 0, pprHubs = 0;
   bool weighted = false;
   int blocksRound[2] = {0, 0};   // BFS/SSSP round grid per W class
   int64_t bytes = 0;
@@ -160,6 +164,7 @@ class Server {
   uint64_t nextTicket = 1;
   gas_server_stats stats;
   std::atomic<int64_t> bytesInUse{0};
+  std::atomic<int64_t> launches{0};  // kernels launched (scheduler thread)
   std::thread sched;
   bool stop = false;
 
@@ -180,13 +185,22 @@ class Server {
 
 Batch::~Batch() {}
 
+// Queries per vertex row of a batch of n: BFS/SSSP at least 32 (a word of
+// query bits), PPR the next power of two.
+int row_width(int kind, int n) {
+  int Q = kind == 2 ? 1 : 32;
+  while (Q < n) Q *= 2;
+  return Q;
+}
+
 int64_t Server::state_bytes(const ServeGraph &g, int kind, int Q) const {
-  const int64_t V = std::max(g.bg.g.nV, 1), W = Q / 32;
+  const int64_t V = std::max(g.bg.g.nV, 1), W = std::max(Q / 32, 1);
   // control words, sources, and up to 16 arrays each rounded up to 256 bytes
   const int64_t base = 256 + 4 * kMaxQ + 16 * 256;
-  if (kind == 0) return base + V * Q * 4 + 16 * V * W + 16 * V;
-  if (kind == 1) return base + V * Q * 4 + 12 * V * W + 16 * V;
-  return base + V * Q * 16 + 2 * V + 64;
+  const int64_t lists = 24 * gas::detail::batch_list_capacity(V, g.bg.g.nE) + 4 * V;
+  if (kind == 0) return base + V * Q * 4 + 16 * V * W + lists;
+  if (kind == 1) return base + V * Q * 4 + 12 * V * W + lists;
+  return base + V * Q * 16 + (int64_t)g.pprSlots * Q * 4 + (int64_t)g.pprHubs * 4;
 }
 
 int64_t Server::available_bytes() {
@@ -262,7 +276,8 @@ Server::~Server() {
     if (!g) continue;
     gas_batch_destroy(g->batch);
     if (g->outDegree) cudaFree(g->outDegree);
-    if (g->order) cudaFree(g->order);
+    if (g->lastActive) cudaFree(g->lastActive);
+    if (g->pprMem) cudaFree(g->pprMem);
     delete g;
   }
   if (mirrors) cudaFreeHost(mirrors);
@@ -279,10 +294,30 @@ void round_pair(const gas::detail::BatchArgs &a, int r, unsigned *done, int bloc
   gas::detail::batch_tail_kernel<W><<<blocks, 256, 0, s>>>(a, r, done);
 }
 
-template <int W>
-void ppr_round(const gas::detail::PprArgs &a, int r, int blocks, cudaStream_t s) {
-  gas::detail::ppr_round_kernel<W><<<blocks, 256, 0, s>>>(a, r);
+template <int QP>
+void ppr_round_launch(const gas::detail::PprArgs &a, int r, int blocks, cudaStream_t s) {
+  gas::detail::ppr_round_kernel<QP><<<blocks, 256, 0, s>>>(a, r);
 }
+
+template <int QP>
+void ppr_start_launch(const gas::detail::PprArgs &a, int blocks, cudaStream_t s) {
+  gas::detail::ppr_init_kernel<QP><<<blocks, 256, 0, s>>>(a);
+  gas::detail::ppr_sources_kernel<QP><<<1, kMaxQ, 0, s>>>(a);
+}
+
+// FN<QP>(args...) for the batch's PPR row width QP (a power of two <= 256).
+#define GAS_PPR_WIDTH(QPV, FN, ...)               \
+  switch (QPV) {                                  \
+    case 1: FN<1>(__VA_ARGS__); break;            \
+    case 2: FN<2>(__VA_ARGS__); break;            \
+    case 4: FN<4>(__VA_ARGS__); break;            \
+    case 8: FN<8>(__VA_ARGS__); break;            \
+    case 16: FN<16>(__VA_ARGS__); break;          \
+    case 32: FN<32>(__VA_ARGS__); break;          \
+    case 64: FN<64>(__VA_ARGS__); break;          \
+    case 128: FN<128>(__VA_ARGS__); break;        \
+    default: FN<256>(__VA_ARGS__); break;         \
+  }
 
 void enqueue_round(Batch &b, int r, int blocks) {
   unsigned *done = &b.ctl->done;
@@ -305,12 +340,7 @@ void enqueue_round(Batch &b, int r, int blocks) {
 }
 
 void enqueue_ppr_round(Batch &b, int r, int blocks) {
-  switch (b.W) {
-    case 1: ppr_round<1>(b.pa, r, blocks, b.stream); break;
-    case 2: ppr_round<2>(b.pa, r, blocks, b.stream); break;
-    case 4: ppr_round<4>(b.pa, r, blocks, b.stream); break;
-    default: ppr_round<8>(b.pa, r, blocks, b.stream); break;
-  }
+  GAS_PPR_WIDTH(b.Q, ppr_round_launch, b.pa, r, blocks, b.stream)
 }
 
 int round_blocks(const Server &s, int64_t warpsOfWork) {
@@ -329,15 +359,21 @@ void Server::issue_chunk(int l, int rounds, bool final) {
     const int32_t *val = b.kind == 2 ? reinterpret_cast<const int32_t *>(b.pa.rank[kPprRounds & 1])
                                      : b.ba.value;
     dim3 tb(32, 8), tg((V + 31) / 32, (b.Q + 31) / 32);
-    if (V > 0) gas::detail::batch_transpose_kernel<<<tg, tb, 0, b.stream>>>(val, V, b.Q, b.nQ, b.out);
+    if (V > 0) {
+      gas::detail::batch_transpose_kernel<<<tg, tb, 0, b.stream>>>(val, V, b.Q, b.nQ, b.out);
+      launches += 1;
+    }
   } else if (b.kind == 2) {
-    const int blocks = round_blocks(*this, V);
+    const int G = 32 / std::min(b.Q, 32);  // units per warp
+    const int blocks = round_blocks(*this, (b.g->pprUnits + G - 1) / G);
     for (int k = 0; k < rounds; ++k) enqueue_ppr_round(b, b.roundsIssued + k, blocks);
     b.roundsIssued += rounds;
+    launches += rounds;
   } else {
     const int blocks = round_blocks(*this, std::max<int64_t>(b.g->bg.nUnits, V));
     for (int k = 0; k < rounds; ++k) enqueue_round(b, b.roundsIssued + k, blocks);
     b.roundsIssued += rounds;
+    launches += 2 * rounds;
   }
   int mi = 0;
   while (L.marks[mi].busy) ++mi;  // at most 2 in flight of 3
@@ -388,30 +424,31 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     memset(&a, 0, sizeof(a));
     a.nVertices = V;
     a.nQueries = b.nQ;
-    a.inOffsets = g.bg.g.inOff;
     a.inSources = g.bg.g.inSrc;
     a.outDegree = g.outDegree;
-    a.order = g.order;
+    a.lastActive = g.lastActive;
+    const size_t nu = (size_t)std::max(g.pprUnits, 1), ns = (size_t)std::max(g.pprSlots, 1);
+    a.nUnits = g.pprUnits;
+    a.unitV = g.pprMem;
+    a.unitBeg = a.unitV + nu;
+    a.unitLen = a.unitBeg + nu;
+    a.unitSlot = a.unitLen + nu;
+    a.slotFirst = a.unitSlot + nu;
+    a.slotCount = a.slotFirst + ns;
+    a.slotHub = a.slotCount + ns;
     a.sources = b.sources;
     for (int k = 0; k < 2; ++k) {
       a.rank[k] = reinterpret_cast<float *>(take(Vs * b.Q * 4));
       a.contrib[k] = reinterpret_cast<float *>(take(Vs * b.Q * 4));
-      a.active[k] = take(Vs);
     }
+    a.partial = reinterpret_cast<float *>(take((size_t)g.pprSlots * b.Q * 4));
+    a.arrive = reinterpret_cast<unsigned *>(take((size_t)g.pprHubs * 4));
+    if (g.pprHubs > 0) cudaMemsetAsync(a.arrive, 0, (size_t)g.pprHubs * 4, b.stream);
     if (p - b.state > b.stateBytes) return fail(GAS_ERR_STATE, "batch state layout overflow");
     a.teleport = 0.15f;
     a.damp = 1.0f - a.teleport;  // as PPR::apply computes it, in float
     const int blocks = 4 * sms;
-    switch (b.W) {
-      case 1: gas::detail::ppr_init_kernel<1><<<blocks, 256, 0, b.stream>>>(a);
-              gas::detail::ppr_sources_kernel<1><<<1, kMaxQ, 0, b.stream>>>(a); break;
-      case 2: gas::detail::ppr_init_kernel<2><<<blocks, 256, 0, b.stream>>>(a);
-              gas::detail::ppr_sources_kernel<2><<<1, kMaxQ, 0, b.stream>>>(a); break;
-      case 4: gas::detail::ppr_init_kernel<4><<<blocks, 256, 0, b.stream>>>(a);
-              gas::detail::ppr_sources_kernel<4><<<1, kMaxQ, 0, b.stream>>>(a); break;
-      default: gas::detail::ppr_init_kernel<8><<<blocks, 256, 0, b.stream>>>(a);
-               gas::detail::ppr_sources_kernel<8><<<1, kMaxQ, 0, b.stream>>>(a); break;
-    }
+    GAS_PPR_WIDTH(b.Q, ppr_start_launch, a, blocks, b.stream)
   } else {
     gas::detail::BatchArgs &a = b.ba;
     memset(&a, 0, sizeof(a));
@@ -429,9 +466,11 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     a.unitEnd = g.bg.unitEnd;
     a.nUnits = g.bg.nUnits;
     a.value = reinterpret_cast<int32_t *>(take(Vs * b.Q * 4));
+    const size_t cap = (size_t)gas::detail::batch_list_capacity(V, g.bg.g.nE);
     for (int k = 0; k < 3; ++k) {
       a.mask[k] = reinterpret_cast<unsigned *>(take(Vs * W * 4));
-      a.list[k] = reinterpret_cast<int32_t *>(take(Vs * 4));
+      a.list[k] = reinterpret_cast<int32_t *>(take(cap * 4));
+      a.listC[k] = reinterpret_cast<int32_t *>(take(cap * 4));
     }
     a.inList = reinterpret_cast<int32_t *>(take(Vs * 4));
     a.seen = b.kind == 0 ? reinterpret_cast<unsigned *>(take(Vs * W * 4)) : nullptr;
@@ -449,8 +488,9 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     gas::detail::batch_init_kernel<<<4 * sms, 256, 0, b.stream>>>(kb, V, b.Q, a.value);
     gas::detail::batch_sources_kernel<<<(b.nQ + 127) / 128, 128, 0, b.stream>>>(
         kb, b.nQ, b.Q, b.W, b.sources, a.value, a.mask[0], a.seen, g.bg.g.outOff, a.inList,
-        a.list[0], a.listCnt);
+        a.list[0], a.listC[0], a.listCnt);
   }
+  launches += 2;  // init + sources
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch start");
   L.batch = bp;
@@ -559,9 +599,7 @@ bool Server::admit() {
       int nQ = (int)std::min<size_t>(pq.size(), (size_t)cfg.maxBatch);
       const int64_t avail = available_bytes();
       auto need = [&](int n) {
-        int Q = 32;
-        while (Q < n) Q *= 2;
-        return state_bytes(*g, kind, Q) + (int64_t)std::max(g->bg.g.nV, 1) * n * 4;
+        return state_bytes(*g, kind, row_width(kind, n)) + (int64_t)std::max(g->bg.g.nV, 1) * n * 4;
       };
       bool shrunk = false;
       while (nQ > 0 && need(nQ) > avail) {
@@ -591,9 +629,8 @@ bool Server::admit() {
       bp->g = g;
       bp->kind = kind;
       bp->nQ = nQ;
-      bp->Q = 32;
-      while (bp->Q < nQ) bp->Q *= 2;
-      bp->W = bp->Q / 32;
+      bp->Q = row_width(kind, nQ);
+      bp->W = std::max(bp->Q / 32, 1);
       bp->stateBytes = state_bytes(*g, kind, bp->Q);
       bp->outBytes = (int64_t)std::max(g->bg.g.nV, 1) * nQ * 4;
       bp->unfetched = nQ;
@@ -655,6 +692,85 @@ void Server::loop() {
       if (!waiting && !stop) cvWork.wait_for(lk, std::chrono::milliseconds(2));
     }
   }
+}
+
+}  // namespace
+
+namespace {
+
+// PPR structures of a graph: out-degrees; work units (a vertex's in-edges,
+// hubs cut into kPprChunk-edge chunks with partial-sum slots), ordered
+// longest first by a counting sort; and lastActive[v], the last of the
+// kPprRounds rounds in which v is active, from kPprRounds - 1 pull steps
+// of the source-independent active sets on the device.
+gas_status build_ppr(ServeGraph &g, int sms) {
+  constexpr int C = gas::detail::kPprChunk;
+  const int32_t V = g.bg.g.nV;
+  const std::vector<int32_t> &inOff = *g.bg.g.hInOff, &outOff = *g.bg.g.hOutOff;
+  std::vector<int32_t> deg((size_t)std::max(V, 1), 0);
+  for (int32_t v = 0; v < V; ++v) deg[v] = outOff[(size_t)v + 1] - outOff[v];
+  std::vector<int32_t> uv, ub, ul, us, sf, sc, sh;
+  uv.reserve(V);
+  ub.reserve(V);
+  ul.reserve(V);
+  us.reserve(V);
+  int32_t hubs = 0;
+  for (int32_t v = 0; v < V; ++v) {
+    const int32_t b = inOff[v], d = inOff[(size_t)v + 1] - b;
+    if (d <= C) {
+      uv.push_back(v); ub.push_back(b); ul.push_back(d); us.push_back(-1);
+      continue;
+    }
+    const int32_t n = (d + C - 1) / C, first = (int32_t)sf.size();
+    for (int32_t c = 0; c < n; ++c) {
+      uv.push_back(v); ub.push_back(b + c * C); ul.push_back(std::min(C, d - c * C));
+      us.push_back(first + c);
+      sf.push_back(first); sc.push_back(n); sh.push_back(hubs);
+    }
+    ++hubs;
+  }
+  const size_t nu = uv.size(), ns = sf.size();
+  // counting sort by length, longest first (stable)
+  std::vector<int64_t> pos((size_t)C + 2, 0);
+  for (size_t i = 0; i < nu; ++i) ++pos[(size_t)(C - ul[i]) + 1];
+  for (size_t k = 1; k < pos.size(); ++k) pos[k] += pos[k - 1];
+  std::vector<int32_t> mem(4 * std::max<size_t>(nu, 1) + 3 * std::max<size_t>(ns, 1), 0);
+  const size_t nuA = std::max<size_t>(nu, 1), nsA = std::max<size_t>(ns, 1);
+  for (size_t i = 0; i < nu; ++i) {
+    const size_t p = (size_t)pos[(size_t)(C - ul[i])]++;
+    mem[p] = uv[i];
+    mem[nuA + p] = ub[i];
+    mem[2 * nuA + p] = ul[i];
+    mem[3 * nuA + p] = us[i];
+  }
+  for (size_t i = 0; i < ns; ++i) {
+    mem[4 * nuA + i] = sf[i];
+    mem[4 * nuA + nsA + i] = sc[i];
+    mem[4 * nuA + 2 * nsA + i] = sh[i];
+  }
+  g.pprUnits = (int32_t)nu;
+  g.pprSlots = (int32_t)ns;
+  g.pprHubs = hubs;
+  uint8_t *tmp = nullptr;
+  const size_t Vs = (size_t)std::max(V, 1);
+  cudaError_t e = cudaMalloc(&g.outDegree, 4 * Vs);
+  if (e == cudaSuccess) e = cudaMalloc(&g.pprMem, 4 * mem.size());
+  if (e == cudaSuccess) e = cudaMalloc(&g.lastActive, Vs);
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, 2 * Vs);
+  if (e == cudaSuccess) e = cudaMemcpy(g.outDegree, deg.data(), 4 * Vs, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(g.pprMem, mem.data(), 4 * mem.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(g.lastActive, 0, Vs);
+  if (e == cudaSuccess) e = cudaMemset(tmp, 1, Vs);  // A0: every vertex
+  for (int k = 1; k < kPprRounds && e == cudaSuccess && V > 0; ++k) {
+    uint8_t *cur = tmp + ((k - 1) & 1) * Vs, *nxt = tmp + (k & 1) * Vs;
+    gas::detail::ppr_active_step_kernel<<<4 * sms, 256>>>(V, g.bg.g.inOff, g.bg.g.inSrc, cur, nxt,
+                                                           g.lastActive, k);
+    e = cudaGetLastError();
+  }
+  // the legacy default stream: ordered after the memsets, not with the lanes
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (tmp) cudaFree(tmp);
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "PPR graph structures");
 }
 
 }  // namespace
@@ -723,28 +839,12 @@ gas_status gas_server_add_graph(gas_server *h, int32_t nVertices, int32_t nEdges
   if (st == GAS_OK) st = gas_batch_set_graph(g->batch, nVertices, nEdges, srcs, dsts, weights);
   if (st == GAS_OK && !gas::internal::batch_graph(g->batch, &g->bg))
     st = fail(GAS_ERR_STATE, "graph upload");
-  if (st == GAS_OK) {
-    const int32_t V = nVertices;
-    const std::vector<int32_t> &inOff = *g->bg.g.hInOff, &outOff = *g->bg.g.hOutOff;
-    std::vector<int32_t> deg(std::max(V, 1), 0), order(std::max(V, 1), 0);
-    for (int32_t v = 0; v < V; ++v) {
-      deg[v] = outOff[(size_t)v + 1] - outOff[v];
-      order[v] = v;
-    }
-    std::stable_sort(order.begin(), order.begin() + V, [&](int32_t a, int32_t b) {
-      return inOff[(size_t)a + 1] - inOff[a] > inOff[(size_t)b + 1] - inOff[b];
-    });
-    cudaError_t e = cudaMalloc(&g->outDegree, 4 * deg.size());
-    if (e == cudaSuccess) e = cudaMalloc(&g->order, 4 * order.size());
-    if (e == cudaSuccess)
-      e = cudaMemcpy(g->outDegree, deg.data(), 4 * deg.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(g->order, order.data(), 4 * order.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) st = cuda_fail(e, "graph upload");
-  }
+  if (st == GAS_OK) st = build_ppr(*g, s.sms);
   if (st != GAS_OK) {
     gas_batch_destroy(g->batch);
     if (g->outDegree) cudaFree(g->outDegree);
-    if (g->order) cudaFree(g->order);
+    if (g->lastActive) cudaFree(g->lastActive);
+    if (g->pprMem) cudaFree(g->pprMem);
     delete g;
     return st;
   }
@@ -865,6 +965,7 @@ gas_status gas_server_get_stats(gas_server *h, gas_server_stats *st) {
   std::lock_guard<std::mutex> lk(s.mu);
   *st = s.stats;
   st->bytesInUse = s.bytesInUse.load();
+  st->kernelLaunches = s.launches.load();
   return GAS_OK;
 }
 
