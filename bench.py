@@ -562,28 +562,41 @@ def run_batch_c4(args):
     stream = torch.cuda.current_stream()
     rng = np.random.default_rng(SEED)
     nq = 256
-    gs = [("rmat21", graphs.rmat(21, 16, seed=SEED, symmetrize=True, weights=(1, 255))),
-          ("grid1024", graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100)))]
+    sc, side = args.rmat_scale or 21, args.grid_side
+    gs = [(f"rmat{sc}", graphs.rmat(sc, 16, seed=SEED, symmetrize=True, weights=(1, 255))),
+          (f"grid{side}", graphs.grid(side, side, 0.15, seed=SEED, weights=(1, 100)))]
+    only = set(args.c4_sets.split(",")) if args.c4_sets else None
     sets = []
     for name, g in gs:
         b = gas.GASBatch(device=local, stream=stream.cuda_stream)
         b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
-        tuned = {}
         for prog in (PROGRAM_BFS, PROGRAM_SSSP):
             src = rng.integers(0, g.n_vertices, nq).astype(np.int32)
-            tuned[prog] = b.autotune(prog, nq)
-            sets.append((name, g, b, prog, src, tuned[prog]))
+            key = f"{name}-{'bfs' if prog == PROGRAM_BFS else 'sssp'}"
+            if only is not None and key not in only:
+                continue
+            if args.no_autotune:
+                cfg = (256, 0, args.c4_delta if prog == PROGRAM_SSSP else 0)
+            else:
+                cfg = b.autotune(prog, nq) + (b.get_delta() if prog == PROGRAM_SSSP else 0,)
+            sets.append((name, g, b, prog, src, cfg))
+    per_set_ms = [0.0] * len(sets)
+    per_set_rounds = [0] * len(sets)
+
     def batched_step():
         ms = 0.0
-        for name, g, b, prog, src, cfg in sets:
+        for i, (name, g, b, prog, src, cfg) in enumerate(sets):
             b.set_config(cfg[0], cfg[1], True)
-            b.run(prog, src, want_results=False)
+            b.set_delta(cfg[2])
+            _, per_set_rounds[i] = b.run(prog, src, want_results=False)
             ms += b.last_ms()
+            per_set_ms[i] += b.last_ms()
         return ms
     for _ in range(args.warmup):
         batched_step()
     barrier(world)
     torch.cuda.synchronize()
+    per_set_ms[:] = [0.0] * len(sets)
     with ClockSampler(local) as clk:
         step_ms = [batched_step() for _ in range(args.steps)]
     total_ms = allreduce_max(world, float(sum(step_ms)))
@@ -593,6 +606,7 @@ def run_batch_c4(args):
     t0 = time.perf_counter()
     for name, g, b, prog, src, cfg in sets:
         b.set_config(cfg[0], cfg[1], True)
+        b.set_delta(cfg[2])
         b.run(prog, src, want_results=True)
     e2e_s = time.perf_counter() - t0
     e2e_value = len(sets) * nq / e2e_s
@@ -601,7 +615,11 @@ def run_batch_c4(args):
     sample = 8
     single_ms, single_n = 0.0, 0
     parity = True
-    for name, g, b, prog, src, cfg in sets:
+    per_set = {}
+    for i, (name, g, b, prog, src, cfg) in enumerate(sets):
+        s_ms0 = single_ms
+        b.set_config(cfg[0], cfg[1], True)
+        b.set_delta(cfg[2])
         batch_out, _ = b.run(prog, src[:sample])
         e = gas.GASEngine(prog, device=local, stream=stream.cuda_stream)
         for q, s0 in enumerate(src[:sample]):
@@ -616,6 +634,11 @@ def run_batch_c4(args):
             e.get_results()  # into the array borrowed by set_graph
             parity &= bool(np.array_equal(e.vertex_data, batch_out[q]))
         e.close()
+        key = f"{name}-{'bfs' if prog == PROGRAM_BFS else 'sssp'}"
+        per_set[key] = {"batched_ms_per_256": per_set_ms[i] / args.steps,
+                        "batched_rounds": per_set_rounds[i],
+                        "single_ms": (single_ms - s_ms0) / sample,
+                        "speedup": ((single_ms - s_ms0) / sample * nq) / (per_set_ms[i] / args.steps)}
     single_qps = single_n / (single_ms / 1e3)
     if rank != 0:
         return
@@ -631,6 +654,7 @@ def run_batch_c4(args):
                    "l2": "inputs (R-MAT-21 CSC/CSR, 2 GB query state) larger than L2"},
         "one_at_a_time": {"value": single_qps, "unit": "queries/s", "sample_queries": single_n,
                           "speedup": value / single_qps, "results_identical": parity},
+        "per_set": per_set,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * nq * len(sets),
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": 5 * len(sets) * args.steps,
@@ -853,7 +877,15 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sssp-grid1024")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--rmat-scale", type=int, default=None,
-                    help="smaller R-MAT scale for the R-MAT-22 workloads (profiling captures)")
+                    help="smaller R-MAT scale for the R-MAT workloads (profiling captures)")
+    ap.add_argument("--grid-side", type=int, default=1024,
+                    help="lattice side of batch-c4 (smaller for profiling captures)")
+    ap.add_argument("--c4-sets", default=None,
+                    help="batch-c4: comma-separated subset of sets, e.g. grid1024-sssp")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch-c4: default launch configuration instead of the autotuner")
+    ap.add_argument("--c4-delta", type=int, default=0,
+                    help="batch-c4 with --no-autotune: SSSP bucket width")
     args = ap.parse_args()
     if args.rmat_scale:
         for k in RMAT_SCALE:

@@ -209,7 +209,8 @@ GAS_API gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries
 GAS_API gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocksPerSM,
                                         int32_t useGraphs);
 /* Times the candidate configurations on nQueries random sources and keeps
- * the fastest; reports the chosen chunk size and CTAs per SM. */
+ * the fastest; reports the chosen chunk size and CTAs per SM (for SSSP it
+ * first chooses the bucket width, see gas_batch_set_delta). */
 GAS_API gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
                                       int32_t *chunkEdges, int32_t *blocksPerSM);
 /* Round policy: a round pushes from the vertices that changed last round
@@ -217,6 +218,19 @@ GAS_API gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQu
  * pulls over every vertex (default alpha 10; 0 = always push).  Results do
  * not depend on it. */
 GAS_API gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha);
+/* SSSP bucket width: 0 relaxes every changed (vertex, query) pair each
+ * round (Bellman-Ford rounds, the reference's order); delta > 0 relaxes a
+ * query's pairs in order of distance, delta at a time (delta-stepping),
+ * which cuts repeated relaxations on high-diameter weighted graphs.
+ * Results do not depend on it.  gas_batch_autotune sets it for SSSP. */
+GAS_API gas_status gas_batch_set_delta(gas_batch *b, int32_t delta);
+/* Frontier representation: 0 = changed vertices with query masks (any
+ * graph); 1 = changed (vertex, query) pairs, one lane each (used when every
+ * out-degree is <= 64 and vertices x queries < 2^31, else masks); -1 =
+ * automatic (the default: pairs where allowed).  Results do not depend on
+ * it. */
+GAS_API gas_status gas_batch_set_frontier(gas_batch *b, int32_t mode);
+GAS_API gas_status gas_batch_get_delta(gas_batch *b, int32_t *delta);
 /* Device milliseconds of the most recent gas_batch_run. */
 GAS_API gas_status gas_batch_last_ms(gas_batch *b, float *ms);
 

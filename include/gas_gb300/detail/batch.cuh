@@ -66,6 +66,24 @@ struct BatchArgs {
   unsigned *errWord;
   int32_t *roundsOut;
   int32_t maxRounds;       // 0 = until nothing changes
+  // SSSP bucket order (delta-stepping; persistent kernel only): a changed
+  // (u, q) is relaxed once dist[u][q] < thresh[q]; others wait in the
+  // changed set.  A query's bound grows by delta after a round in which it
+  // produced no value below the bound.  0 = every changed pair every round.
+  int32_t delta;
+  int32_t *thresh[2];      // [Q] by round parity
+  unsigned *nearFlag[3];   // [W] queries with a new value below the bound (rotating)
+  // Pair frontier (graphs of small out-degree, V * Q < 2^31): the changed
+  // set is a list of (vertex, query) entries u * Q + q, one lane each,
+  // instead of vertex entries with query masks; every round pushes.
+  uint32_t *pairs[3];      // [V * Q] each (rotating, counts in listCnt >> 32)
+  int32_t pairMode;
+};
+
+// Shared-memory view of the bucket bounds for one round (null when off).
+struct BatchBucket {
+  const int32_t *bound;  // [Q] this round's thresh
+  unsigned *near;        // [W] block-local near flags
 };
 
 constexpr int32_t kBatchInf = 0x7fffffff - 100000;  // SSSP gatherZero (sssp.cu:32-33)
@@ -212,23 +230,45 @@ __device__ __forceinline__ void batch_push_unit(const BatchArgs &a, int u, int c
                                                 const unsigned *cur, unsigned *nxt,
                                                 int32_t *listNext, int32_t *listNextC,
                                                 unsigned long long *cntNext,
-                                                unsigned long long &changed) {
+                                                unsigned long long &changed,
+                                                const BatchBucket bk = BatchBucket{nullptr, nullptr}) {
   const int lane = threadIdx.x & 31;
   const int Q = W * 32;
   unsigned m[W];
-  int nbits = 0, nwords = 0;
 #pragma unroll
-  for (int k = 0; k < W; ++k) {
-    m[k] = __ldcg(cur + (size_t)u * W + k);
-    nbits += __popc(m[k]);
-    nwords += m[k] != 0u;
-  }
+  for (int k = 0; k < W; ++k) m[k] = __ldcg(cur + (size_t)u * W + k);
   int du[W];
   if (KIND == kBatchSSSP) {
 #pragma unroll
     for (int k = 0; k < W; ++k)
       du[k] = ((m[k] >> lane) & 1u) ? __ldcg(a.value + (size_t)u * Q + k * 32 + lane) : kBatchInf;
   }
+  bool deferred = false;
+  if (KIND == kBatchSSSP && bk.bound) {  // relax below the bound now, keep the rest
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const unsigned nearM =
+          __ballot_sync(kFullMask, ((m[k] >> lane) & 1u) && du[k] < bk.bound[k * 32 + lane]);
+      const unsigned far = m[k] & ~nearM;
+      m[k] = nearM;
+      if (far) {
+        deferred = true;
+        if (lane == 0) {
+          atomicOr(nxt + (size_t)u * W + k, far);
+          changed += __popc(far);
+        }
+      }
+    }
+  }
+  int nbits = 0, nwords = 0;
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    nbits += __popc(m[k]);
+    nwords += m[k] != 0u;
+  }
+  unsigned nearW[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) nearW[k] = 0u;
   const int ub = a.outOffsets[u];
   const int eb = ub + chunk * kPushChunk;
   const int ee = min(eb + kPushChunk, a.outOffsets[u + 1]);
@@ -277,7 +317,10 @@ __device__ __forceinline__ void batch_push_unit(const BatchArgs &a, int u, int c
                           : kBatchInf;
 #pragma unroll
           for (int t = 0; t < 4; ++t)
-            if (ok && bs[t] >= 0 && ds[t] + w < olds[t]) imp |= 1u << bs[t];
+            if (ok && bs[t] >= 0 && ds[t] + w < olds[t]) {
+              imp |= 1u << bs[t];
+              if (bk.bound && ds[t] + w < bk.bound[k * 32 + bs[t]]) nearW[k] |= 1u << bs[t];
+            }
         }
         if (imp) {
           atomicOr(nxt + (size_t)v * W + k, imp);
@@ -299,6 +342,7 @@ __device__ __forceinline__ void batch_push_unit(const BatchArgs &a, int u, int c
             const int cand = du[k] + wt;
             const int old = atomicMin(a.value + (size_t)vt * Q + k * 32 + lane, cand);
             imp = cand < old;
+            if (imp && bk.bound && cand < bk.bound[k * 32 + lane]) nearW[k] |= 1u << lane;
           }
           const unsigned word = __ballot_sync(kFullMask, imp);
           if (word) {
@@ -316,6 +360,91 @@ __device__ __forceinline__ void batch_push_unit(const BatchArgs &a, int u, int c
     if (any) want = atomicExch(a.inList + v, round + 1) != round + 1;
     warp_append(want, v, want ? a.outOffsets[v + 1] - a.outOffsets[v] : 0, listNext, listNextC,
                 cntNext);
+  }
+  if (KIND == kBatchSSSP && bk.bound) {
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const unsigned nw = __reduce_or_sync(kFullMask, nearW[k]);
+      if (lane == 0 && nw) atomicOr(bk.near + k, nw);
+    }
+    // u keeps its deferred queries: back on the next list (all its chunks)
+    bool wantU = false;
+    if (deferred && lane == 0) wantU = atomicExch(a.inList + u, round + 1) != round + 1;
+    warp_append(wantU, u, wantU ? a.outOffsets[u + 1] - ub : 0, listNext, listNextC, cntNext);
+  }
+}
+
+// Appends each lane's entry (when `want`) to a pair list: one atomic per
+// warp.  Warp-uniform call.
+__device__ __forceinline__ void warp_append_pair(bool want, uint32_t entry, uint32_t *list,
+                                                 unsigned long long *cnt) {
+  const int lane = threadIdx.x & 31;
+  const unsigned who = __ballot_sync(kFullMask, want);
+  if (!who) return;
+  unsigned long long base = 0ull;
+  if (lane == 0) base = atomicAdd(cnt, (unsigned long long)__popc(who) << 32);
+  base = __shfl_sync(kFullMask, base, 0) >> 32;
+  if (want) list[base + __popc(who & ((1u << lane) - 1u))] = entry;
+}
+
+// Pair-frontier push: lane i takes entry i of the current pair list (when
+// `valid`), a changed (u, q), and relaxes u's out-edges for q alone; a
+// destination whose value changes is appended as (v, q) the first time its
+// query bit is set this round.  Warp-uniform (lanes step through their
+// edges together, up to the warp's largest out-degree).
+template <int W, int KIND>
+__device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, uint32_t entry,
+                                                int round, unsigned *nxt, uint32_t *listNext,
+                                                unsigned long long *cntNext,
+                                                unsigned long long &changed,
+                                                const BatchBucket bk) {
+  constexpr int Q = 32 * W;
+  constexpr int LOGQ = W == 1 ? 5 : W == 2 ? 6 : W == 4 ? 7 : 8;
+  const int u = valid ? (int)(entry >> LOGQ) : 0;
+  const int q = (int)(entry & (Q - 1));
+  const unsigned bit = 1u << (q & 31);
+  const int wq = q >> 5;
+  int eb = valid ? a.outOffsets[u] : 0;
+  int deg = valid ? a.outOffsets[u + 1] - eb : 0;
+  int du = 0;
+  bool keep = false;
+  if (KIND == kBatchSSSP && valid) {
+    du = __ldcg(a.value + (size_t)u * Q + q);
+    if (bk.bound && du >= bk.bound[q]) {  // not this bucket: keep (u, q) for later
+      const unsigned old = atomicOr(nxt + (size_t)u * W + wq, bit);
+      keep = !(old & bit);
+      changed += 1;
+      deg = 0;
+    }
+  }
+  if (KIND == kBatchSSSP && bk.bound) warp_append_pair(keep, entry, listNext, cntNext);
+  const int maxDeg = __reduce_max_sync(kFullMask, deg);
+  for (int j = 0; j < maxDeg; ++j) {
+    bool want = false;
+    uint32_t out = 0u;
+    if (j < deg) {
+      const int v = __ldg(a.outDests + eb + j);
+      if (KIND == kBatchBFS) {
+        const unsigned old = atomicOr(a.seen + (size_t)v * W + wq, bit);
+        if (!(old & bit)) {
+          a.value[(size_t)v * Q + q] = round + 1;
+          want = true;
+        }
+      } else {
+        const int cand = du + __ldg(a.weightsOut + eb + j);
+        const int old = atomicMin(a.value + (size_t)v * Q + q, cand);
+        if (cand < old) {
+          const unsigned o2 = atomicOr(nxt + (size_t)v * W + wq, bit);
+          want = !(o2 & bit);
+          if (bk.bound && cand < bk.bound[q] && !(bk.near[wq] & bit)) atomicOr(bk.near + wq, bit);
+        }
+      }
+      if (want) {
+        changed += 1;
+        out = ((uint32_t)v << LOGQ) | (uint32_t)q;
+      }
+    }
+    warp_append_pair(want, out, listNext, cntNext);
   }
 }
 
@@ -342,12 +471,32 @@ __device__ __forceinline__ void batch_compact(const BatchArgs &a, const unsigned
 
 template <int W, int KIND>
 __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
+  __shared__ int32_t sBound[32 * W];
+  __shared__ unsigned sNear[W];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const size_t maskWords = (size_t)a.nVertices * W;
+  const bool buckets = KIND == kBatchSSSP && a.delta > 0;
+  const BatchBucket bk{buckets ? sBound : nullptr, buckets ? sNear : nullptr};
   int r = 0;
   for (;; ++r) {
     if (a.maxRounds > 0 && r >= a.maxRounds) break;
+    if (buckets) {
+      // this round's bounds: last round's, plus delta for the queries that
+      // produced no value below theirs (every block computes the same)
+      const int32_t *tPrev = (r & 1) ? a.thresh[1] : a.thresh[0];
+      int32_t *tNext = (r & 1) ? a.thresh[0] : a.thresh[1];
+      const unsigned *nPrev = a.nearFlag[(r + 2) % 3];  // written in round r - 1
+      for (int q = threadIdx.x; q < 32 * W; q += blockDim.x) {
+        int32_t t = __ldcg(tPrev + q);
+        if (r > 0 && !((__ldcg(nPrev + q / 32) >> (q % 32)) & 1u)) t += a.delta;
+        sBound[q] = t;
+        if (blockIdx.x == 0) tNext[q] = t;
+      }
+      if (threadIdx.x < W) sNear[threadIdx.x] = 0u;
+      if (blockIdx.x == 0 && threadIdx.x < W) a.nearFlag[(r + 1) % 3][threadIdx.x] = 0u;
+      __syncthreads();
+    }
     const unsigned *cur = a.mask[r % 3];
     unsigned *nxt = a.mask[(r + 1) % 3];
     unsigned *clr = a.mask[(r + 2) % 3];
@@ -360,7 +509,7 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
     const unsigned long long lc = a.listCnt[rc];
     const long long nList = (long long)(lc >> 32);
     const long long eOut = (long long)(lc & 0xffffffffull);
-    const bool push = eOut * a.alpha <= (long long)a.nEdges;
+    const bool push = a.pairMode || buckets || eOut * a.alpha <= (long long)a.nEdges;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       a.cnt[rn] = 0ull;
       a.listCnt[(r + 2) % 3] = 0ull;  // input of round r-1, appended in round r+1
@@ -369,16 +518,30 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
          i += (size_t)gridDim.x * blockDim.x)
       clr[i] = 0u;
     unsigned long long changed = 0ull;
-    if (push) {
+    if (a.pairMode) {
+      const uint32_t *pc = a.pairs[rc];
+      uint32_t *pn = a.pairs[rn];
+      const long long threads = (long long)gridDim.x * blockDim.x;
+      for (long long base = gw * 32; base < nList; base += threads) {
+        const long long i = base + (threadIdx.x & 31);
+        const bool valid = i < nList;
+        batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, nxt, pn, cntNext,
+                                 changed, bk);
+      }
+    } else if (push) {
       for (long long i = gw; i < nList; i += warps)
         batch_push_unit<W, KIND>(a, listCur[i], listCurC[i], r, cur, nxt, listNext, listNextC,
-                                 cntNext, changed);
+                                 cntNext, changed, bk);
     } else {
       for (long long u = gw; u < a.nUnits; u += warps)
         batch_unit<W, KIND>(a, (int)u, r, cur, nxt, changed);
     }
     changed = warp_sum_u64(changed);
     if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + rc, changed);
+    if (buckets) {
+      __syncthreads();
+      if (threadIdx.x < W && sNear[threadIdx.x]) atomicOr(a.nearFlag[rc] + threadIdx.x, sNear[threadIdx.x]);
+    }
     if (!grid_barrier(a.barrier, a.errWord)) break;
     if (a.cnt[rc] == 0ull) break;  // uniform: read after the barrier
     if (!push) {
@@ -390,28 +553,41 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
 }
 
 // value[V][Q] := BFS -1 / SSSP gatherZero; sources get 0 and their bit.
-static __global__ void batch_init_kernel(int kind, int32_t nVertices, int32_t Q, int32_t *value) {
+// thresh0 (may be null): every query's first bucket bound, delta.
+static __global__ void batch_init_kernel(int kind, int32_t nVertices, int32_t Q, int32_t *value,
+                                         int32_t *thresh0 = nullptr, int32_t delta = 0) {
   const size_t n = (size_t)nVertices * Q;
   const int32_t fill = kind == kBatchBFS ? -1 : kBatchInf;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x)
     value[i] = fill;
+  if (thresh0)
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < (size_t)Q;
+         q += (size_t)gridDim.x * blockDim.x)
+      thresh0[q] = delta;
 }
 
 // Sources: value 0, their query bit, and the first list (each source
 // vertex once; inList was reset to -1).
+// With a pair list (pairs0 non-null) the first list is (s_q, q) per query.
 static __global__ void batch_sources_kernel(int kind, int32_t nQueries, int32_t Q, int32_t W,
                                             const int32_t *sources, int32_t *value,
                                             unsigned *mask0, unsigned *seen,
                                             const int32_t *outOffsets, int32_t *inList,
                                             int32_t *list0, int32_t *list0C,
-                                            unsigned long long *listCnt0) {
+                                            unsigned long long *listCnt0,
+                                            uint32_t *pairs0 = nullptr) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nQueries) return;
   const int s = sources[q];
   value[(size_t)s * Q + q] = 0;
   atomicOr(mask0 + (size_t)s * W + q / 32, 1u << (q % 32));
   if (kind == kBatchBFS) atomicOr(seen + (size_t)s * W + q / 32, 1u << (q % 32));
+  if (pairs0) {
+    const unsigned long long pos = atomicAdd(listCnt0, 1ull << 32) >> 32;
+    pairs0[pos] = (uint32_t)s * (uint32_t)Q + (uint32_t)q;
+    return;
+  }
   if (atomicExch(inList + s, 0) != 0) {
     const unsigned d = (unsigned)(outOffsets[s + 1] - outOffsets[s]);
     const unsigned ne = d > 0u ? (d + kPushChunk - 1) / kPushChunk : 1u;

@@ -68,3 +68,44 @@ def test_batch_autotune_and_errors(gpu):
         b.set_graph(g.n_vertices, g.srcs, g.dsts)  # no weights
         with pytest.raises(GasError):
             b.run(PROGRAM_SSSP, np.array([0], np.int32))
+
+
+@pytest.mark.parametrize("delta", [1, 16, 100, 5000])
+def test_batch_sssp_buckets_match_single_source(gpu, port, delta):
+    """Delta-stepping order (distances relaxed a bucket at a time, far pairs
+    deferred) gives the same distances as Bellman-Ford rounds."""
+    for g in (graphs.grid(40, 36, 0.15, seed=47, weights=(1, 100)),
+              graphs.rmat(11, 16, seed=48, symmetrize=True, weights=(1, 255)),
+              graphs.rmat(10, 8, seed=49, weights=(1, 9))):
+        rng = np.random.default_rng(delta)
+        sources = rng.integers(0, g.n_vertices, 70).astype(np.int32)
+        with GASBatch() as b:
+            b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+            b.set_delta(delta)
+            assert b.get_delta() == delta
+            got, _ = b.run(PROGRAM_SSSP, sources)
+            b.set_delta(0)
+            base, _ = b.run(PROGRAM_SSSP, sources)
+        assert np.array_equal(got, base)
+        check_queries(port, g, PROGRAM_SSSP, sources[::7], got[::7])
+
+
+@pytest.mark.parametrize("delta", [0, 50])
+def test_batch_pair_frontier_matches_masks(gpu, port, delta):
+    """(vertex, query) pair frontier (small out-degree graphs) = vertex-mask
+    frontier = single-source oracle, for BFS and SSSP."""
+    g = graphs.grid(64, 50, 0.15, seed=51, weights=(1, 100))
+    rng = np.random.default_rng(52 + delta)
+    for nq in (5, 33, 256):
+        sources = rng.integers(0, g.n_vertices, nq).astype(np.int32)
+        with GASBatch() as b:
+            b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+            b.set_delta(delta)
+            for program in (PROGRAM_BFS, PROGRAM_SSSP):
+                out = []
+                for mode in (1, 0):
+                    b.set_frontier(mode)
+                    got, rounds = b.run(program, sources)
+                    out.append(got)
+                assert np.array_equal(out[0], out[1])
+                check_queries(port, g, program, sources[::11], out[0][::11])

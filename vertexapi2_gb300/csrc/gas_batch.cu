@@ -29,7 +29,7 @@ namespace {
 constexpr int kMaxBatch = 256;  // queries per launch (8 words of query bits)
 
 struct GraphCache {
-  int kind, W, nQ, blocksPerSM, chunk;
+  int kind, W, nQ, blocksPerSM, chunk, delta, pairs;
   cudaGraphExec_t exec;
 };
 
@@ -44,6 +44,12 @@ struct gas_batch_s {
   int32_t blocksPerSM = 0;  // 0 = as many as fit
   bool useGraphs = true;
   int32_t alpha = 10;  // push round when list out-degree total * alpha <= E
+  int32_t delta = 0;   // SSSP bucket width (0 = Bellman-Ford rounds)
+  int32_t frontier = -1;  // -1 automatic, 0 vertex masks, 1 (vertex, query) pairs
+  int32_t maxOutDeg = 0;
+  uint32_t *pairs[3] = {nullptr, nullptr, nullptr};
+  size_t pairCap = 0;
+  int32_t *bucketMem = nullptr;  // thresh[2][256] | nearFlag[3][8]
   int32_t unitChunk = 0;
   int32_t *list[3] = {nullptr, nullptr, nullptr};
   int32_t *listC[3] = {nullptr, nullptr, nullptr};
@@ -100,8 +106,36 @@ void free_state(gas_batch *b) {
   b->list[0] = b->list[1] = b->list[2] = nullptr;
   b->listC[0] = b->listC[1] = b->listC[2] = nullptr;
   b->inList = nullptr;
+  for (int k = 0; k < 3; ++k) {
+    if (b->pairs[k]) cudaFree(b->pairs[k]);
+    b->pairs[k] = nullptr;
+  }
+  b->pairCap = 0;
   b->capQ = 0;
   drop_graphs(b);
+}
+
+// Pair frontier for graphs whose out-degrees are small (a lane walks a
+// vertex's out-edges alone) and whose V * Q entries fit 32 bits.
+bool use_pairs(const gas_batch *b, const CoreGraph &g, int32_t Q) {
+  const bool allowed = b->maxOutDeg <= 64 && (long long)g.nV * Q < (1ll << 31);
+  return b->frontier == 0 ? false : allowed;
+}
+
+gas_status ensure_pairs(gas_batch *b, const CoreGraph &g, int32_t Q) {
+  const size_t need = (size_t)std::max(g.nV, 1) * Q;
+  if (b->pairCap >= need) return GAS_OK;
+  for (int k = 0; k < 3; ++k) {
+    if (b->pairs[k]) cudaFree(b->pairs[k]);
+    b->pairs[k] = nullptr;
+  }
+  b->pairCap = 0;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMalloc(&b->pairs[k], need * 4);
+  if (e != cudaSuccess) return cuda_fail(e, "batch pair lists");
+  b->pairCap = need;
+  drop_graphs(b);
+  return GAS_OK;
 }
 
 void free_units(gas_batch *b) {
@@ -167,7 +201,7 @@ gas_status ensure_state(gas_batch *b, const CoreGraph &g, int32_t Q) {
 }
 
 template <int W, int KIND>
-gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
+gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks, bool pairs) {
   gas::detail::BatchArgs a;
   memset(&a, 0, sizeof(a));
   a.nVertices = g.nV;
@@ -198,6 +232,13 @@ gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
   a.roundsOut = cv.rounds;
   a.listCnt = cv.listCnt;
   a.maxRounds = 0;
+  a.delta = KIND == gas::detail::kBatchSSSP ? b->delta : 0;
+  a.thresh[0] = b->bucketMem;
+  a.thresh[1] = b->bucketMem + kMaxBatch;
+  for (int k = 0; k < 3; ++k)
+    a.nearFlag[k] = reinterpret_cast<unsigned *>(b->bucketMem + 2 * kMaxBatch + 8 * k);
+  a.pairMode = pairs ? 1 : 0;
+  for (int k = 0; k < 3; ++k) a.pairs[k] = pairs ? b->pairs[k] : nullptr;
   void *args[] = {&a};
   cudaError_t e = cudaLaunchCooperativeKernel((const void *)gas::detail::batch_run_kernel<W, KIND>,
                                               dim3(blocks), dim3(256), args, 0, b->stream);
@@ -205,9 +246,11 @@ gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks) {
 }
 
 template <int W>
-gas_status launch_run_kind(gas_batch *b, const CoreGraph &g, int kind, int32_t Q, int blocks) {
-  return kind == gas::detail::kBatchBFS ? launch_run<W, gas::detail::kBatchBFS>(b, g, Q, blocks)
-                                        : launch_run<W, gas::detail::kBatchSSSP>(b, g, Q, blocks);
+gas_status launch_run_kind(gas_batch *b, const CoreGraph &g, int kind, int32_t Q, int blocks,
+                           bool pairs) {
+  return kind == gas::detail::kBatchBFS
+             ? launch_run<W, gas::detail::kBatchBFS>(b, g, Q, blocks, pairs)
+             : launch_run<W, gas::detail::kBatchSSSP>(b, g, Q, blocks, pairs);
 }
 
 int grid_blocks(gas_batch *b, int kind, int W) {
@@ -227,7 +270,8 @@ int grid_blocks(gas_batch *b, int kind, int W) {
 
 // The whole batch on b->stream: sources (from pinned staging), state reset,
 // initial values, the persistent run, query-major results in outDev.
-gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, int32_t Q) {
+gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, int32_t Q,
+                         bool pairs) {
   const int W = Q / 32;
   const size_t V = (size_t)g.nV;
   cudaError_t e = cudaMemcpyAsync(b->srcDev, b->srcPinned, sizeof(int32_t) * nQ,
@@ -237,21 +281,24 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
   if (e == cudaSuccess) e = cudaMemsetAsync(b->seen, 0, V * W * 4, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->inList, 0xff, V * 4, b->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->ctl, 0, kCtlBytes, b->stream);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b->bucketMem + 2 * kMaxBatch, 0, 4 * 3 * 8, b->stream);
   if (e != cudaSuccess) return cuda_fail(e, "batch reset");
-  gas::detail::batch_init_kernel<<<4 * b->sms, 256, 0, b->stream>>>(kind, g.nV, Q, b->value);
+  gas::detail::batch_init_kernel<<<4 * b->sms, 256, 0, b->stream>>>(kind, g.nV, Q, b->value,
+                                                                     b->bucketMem, b->delta);
   CtlView cv = ctl_view(b);
   gas::detail::batch_sources_kernel<<<(nQ + 127) / 128, 128, 0, b->stream>>>(
       kind, nQ, Q, W, b->srcDev, b->value, b->mask[0], b->seen, g.outOff, b->inList,
-      b->list[0], b->listC[0], cv.listCnt);
+      b->list[0], b->listC[0], cv.listCnt, pairs ? b->pairs[0] : nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch init");
   const int blocks = grid_blocks(b, kind, W);
   gas_status st;
   switch (W) {
-    case 1: st = launch_run_kind<1>(b, g, kind, Q, blocks); break;
-    case 2: st = launch_run_kind<2>(b, g, kind, Q, blocks); break;
-    case 4: st = launch_run_kind<4>(b, g, kind, Q, blocks); break;
-    default: st = launch_run_kind<8>(b, g, kind, Q, blocks); break;
+    case 1: st = launch_run_kind<1>(b, g, kind, Q, blocks, pairs); break;
+    case 2: st = launch_run_kind<2>(b, g, kind, Q, blocks, pairs); break;
+    case 4: st = launch_run_kind<4>(b, g, kind, Q, blocks, pairs); break;
+    default: st = launch_run_kind<8>(b, g, kind, Q, blocks, pairs); break;
   }
   if (st) return st;
   dim3 tb(32, 8), tg((g.nV + 31) / 32, (Q + 31) / 32);
@@ -266,6 +313,11 @@ gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const
   while (Q < nQ) Q *= 2;
   gas_status st = ensure_state(b, g, std::max(Q, 32));
   if (st) return st;
+  const bool pairs = use_pairs(b, g, Q);
+  if (pairs) {
+    st = ensure_pairs(b, g, Q);
+    if (st) return st;
+  }
   memcpy(b->srcPinned, sources, sizeof(int32_t) * nQ);
   cudaEventRecord(b->t0, b->stream);
   bool launched = false;
@@ -273,16 +325,17 @@ gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const
     cudaGraphExec_t exec = nullptr;
     for (auto &c : b->graphs)
       if (c.kind == kind && c.W == Q / 32 && c.nQ == nQ && c.blocksPerSM == b->blocksPerSM &&
-          c.chunk == b->unitChunk)
+          c.chunk == b->unitChunk && c.delta == b->delta && c.pairs == (int)pairs)
         exec = c.exec;
     if (!exec) {
       cudaGraph_t graph = nullptr;
       if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        gas_status cst = enqueue_batch(b, g, kind, nQ, Q);
+        gas_status cst = enqueue_batch(b, g, kind, nQ, Q, pairs);
         cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
         if (cst == GAS_OK && ce == cudaSuccess && graph &&
             cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
-          b->graphs.push_back({kind, Q / 32, nQ, b->blocksPerSM, b->unitChunk, exec});
+          b->graphs.push_back(
+              {kind, Q / 32, nQ, b->blocksPerSM, b->unitChunk, b->delta, (int)pairs, exec});
         } else {
           exec = nullptr;
           b->useGraphs = false;  // this runtime cannot capture the batch: launch directly
@@ -300,7 +353,7 @@ gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const
     }
   }
   if (!launched) {
-    st = enqueue_batch(b, g, kind, nQ, Q);
+    st = enqueue_batch(b, g, kind, nQ, Q, pairs);
     if (st) return st;
   }
   cudaEventRecord(b->t1, b->stream);
@@ -356,6 +409,7 @@ gas_status gas_batch_create(int32_t device, void *stream, gas_batch **out) {
   cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
   cudaError_t e = cudaMalloc(&b->ctl, kCtlBytes);
   if (e == cudaSuccess) e = cudaMemset(b->ctl, 0, kCtlBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&b->bucketMem, 4 * (2 * kMaxBatch + 3 * 8));
   if (e == cudaSuccess) e = cudaMallocHost(&b->srcPinned, sizeof(int32_t) * kMaxBatch);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
@@ -375,6 +429,7 @@ gas_status gas_batch_destroy(gas_batch *b) {
   free_units(b);
   if (b->weightsOut) cudaFree(b->weightsOut);
   if (b->ctl) cudaFree(b->ctl);
+  if (b->bucketMem) cudaFree(b->bucketMem);
   if (b->srcPinned) cudaFreeHost(b->srcPinned);
   if (b->t0) cudaEventDestroy(b->t0);
   if (b->t1) cudaEventDestroy(b->t1);
@@ -396,6 +451,9 @@ gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
   if (st) return st;
   CoreGraph g;
   gas::internal::core_graph(b->core, &g);
+  b->maxOutDeg = 0;
+  for (int32_t v = 0; v < nVertices; ++v)
+    b->maxOutDeg = std::max(b->maxOutDeg, (*g.hOutOff)[(size_t)v + 1] - (*g.hOutOff)[v]);
   st = build_units(b, g, b->chunk);
   if (st || !weights || nEdges == 0) return st;
   // weights in CSR order for push rounds (stable by source, as the CSR)
@@ -460,6 +518,28 @@ gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha) {
   return GAS_OK;
 }
 
+gas_status gas_batch_set_delta(gas_batch *b, int32_t delta) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  if (delta < 0) return fail(GAS_ERR_INVALID, "delta must be >= 0");
+  b->delta = delta;
+  drop_graphs(b);
+  return GAS_OK;
+}
+
+gas_status gas_batch_set_frontier(gas_batch *b, int32_t mode) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  if (mode < -1 || mode > 1) return fail(GAS_ERR_INVALID, "frontier mode must be -1, 0 or 1");
+  b->frontier = mode;
+  drop_graphs(b);
+  return GAS_OK;
+}
+
+gas_status gas_batch_get_delta(gas_batch *b, int32_t *delta) {
+  if (!b || !delta) return fail(GAS_ERR_INVALID, "null argument");
+  *delta = b->delta;
+  return GAS_OK;
+}
+
 gas_status gas_batch_last_ms(gas_batch *b, float *ms) {
   if (!b || !ms) return fail(GAS_ERR_INVALID, "null argument");
   *ms = b->lastMs;
@@ -475,6 +555,25 @@ gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
   std::vector<int32_t> src(nq);
   std::mt19937 rng(12345);
   for (auto &s : src) s = (int32_t)(rng() % (uint32_t)std::max(g.nV, 1));
+  // SSSP: the bucket width first (Bellman-Ford rounds or delta-stepping),
+  // with the current launch configuration
+  if (program == GAS_PROGRAM_SSSP) {
+    const int32_t deltas[] = {0, 128, 512, 2048};
+    float bestD = 1e30f;
+    int32_t bd = b->delta;
+    for (int32_t d : deltas) {
+      gas_status st = gas_batch_set_delta(b, d);
+      int32_t r = 0;
+      if (st == GAS_OK) st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);
+      if (st) return st;
+      if (b->lastMs < bestD) {
+        bestD = b->lastMs;
+        bd = d;
+      }
+    }
+    gas_status st = gas_batch_set_delta(b, bd);
+    if (st) return st;
+  }
   const int32_t chunks[] = {32, 128, 512, 2048};
   const int32_t blocks[] = {0, 2, 1};
   float best = 1e30f;

@@ -207,6 +207,17 @@ class GASBatch:
     def set_policy(self, alpha: int) -> None:
         check(self._lib.gas_batch_set_policy(self._h, alpha), "gas_batch_set_policy")
 
+    def set_frontier(self, mode: int) -> None:
+        check(self._lib.gas_batch_set_frontier(self._h, mode), "gas_batch_set_frontier")
+
+    def set_delta(self, delta: int) -> None:
+        check(self._lib.gas_batch_set_delta(self._h, delta), "gas_batch_set_delta")
+
+    def get_delta(self) -> int:
+        d = C.c_int32()
+        check(self._lib.gas_batch_get_delta(self._h, C.byref(d)), "gas_batch_get_delta")
+        return d.value
+
     def autotune(self, program: int, n_queries: int) -> tuple[int, int]:
         c, b = C.c_int32(), C.c_int32()
         check(self._lib.gas_batch_autotune(self._h, program, n_queries, C.byref(c), C.byref(b)),
