@@ -226,10 +226,12 @@ C5_SWEEP_QUERIES = 512
 C5_LANES = 8                  # batches in flight at once
 
 
-def c5_graphs():
+def c5_graphs(only=None):
     from vertexapi2_gb300 import graphs
     out = []
     for name, sc in C5_GRAPHS:
+        if only and name not in only:
+            continue
         if sc is None:
             g = graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100))
         else:
@@ -774,7 +776,7 @@ def run_serve_c5(args):
     from vertexapi2_gb300._lib import PROGRAM_PPR
     gas.load()
     stream = torch.cuda.current_stream()
-    gs = c5_graphs()
+    gs = c5_graphs(set(args.c5_graphs.split(",")) if args.c5_graphs else None)
     srv = gas.GASServer(device=local, lanes=C5_LANES)
     ids = [srv.add_graph(g.n_vertices, g.srcs, g.dsts, g.weights) for _, g in gs]
     bufs = [(torch.empty(g.n_vertices, dtype=torch.int32).pin_memory().numpy(),
@@ -886,6 +888,8 @@ def main():
                     help="batch-c4: default launch configuration instead of the autotuner")
     ap.add_argument("--c4-delta", type=int, default=0,
                     help="batch-c4 with --no-autotune: SSSP bucket width")
+    ap.add_argument("--c5-graphs", default=None,
+                    help="serve-c5: comma-separated subset of the graphs, e.g. rmat20 (profiling)")
     args = ap.parse_args()
     if args.rmat_scale:
         for k in RMAT_SCALE:
