@@ -422,7 +422,9 @@ def run_ours(args):
     eng = gas.GASEngine(w["program"], device=local, stream=stream.cuda_stream)
     init = w["init"].copy()
     ed = g.weights if w["ed_bytes"] else None
+    t_sg = time.perf_counter()
     eng.set_graph(g.n_vertices, init, g.srcs, g.dsts, ed)
+    set_graph_ms = 1e3 * (time.perf_counter() - t_sg)
     eng.save_vertex_data()
     lo, hi = w["active"]
 
@@ -531,7 +533,8 @@ def run_ours(args):
                    "rmat_scale": RMAT_SCALE.get(args.workload), "n_vertices": g.n_vertices, "n_edges": g.n_edges, "seed": SEED,
                    "rounds": rounds, "edges_traversed_per_run": edges_per_run,
                    "l2": "flushed between timed steps (512 MB write)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "set_graph_ms": set_graph_ms},
         "roofline": {"bound": "hbm", "kernel": "run_persistent_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None,

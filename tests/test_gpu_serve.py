@@ -119,11 +119,16 @@ def test_concurrent_clients(gpu, port):
 def test_admission_shrinks_batches_under_memory_limit(gpu, port):
     import torch
     g = graphs.rmat(16, 16, seed=65, symmetrize=True, weights=(1, 255))
-    free = torch.cuda.mem_get_info(0)[0]
     V = g.n_vertices
-    # room for the graph and a batch of 32 BFS queries (~19 MB), not 64 (~37 MB)
-    graph_bytes = g.n_edges * 20 + V * 24 + (1 << 20)
-    room = graph_bytes + 2 * (V * 32 * 4 + 32 * V * 4 // 8 + 16 * V) + (8 << 20)
+    # device bytes the resident graph takes, measured
+    free0 = torch.cuda.mem_get_info(0)[0]
+    with GASServer(lanes=1, reserve_bytes=0) as probe:
+        probe.add_graph(V, g.srcs, g.dsts, g.weights)
+        graph_bytes = free0 - torch.cuda.mem_get_info(0)[0]
+    free = torch.cuda.mem_get_info(0)[0]
+    # room for the graph and a batch of 32 BFS queries (~20 MB), not 64 (~38 MB)
+    batch32 = V * 32 * 4 * 2 + V * 16 + 24 * (V + g.n_edges // 512) + 4 * V
+    room = graph_bytes + batch32 + (8 << 20)
     with GASServer(lanes=1, reserve_bytes=max(free - room, 0)) as srv:
         gid = srv.add_graph(V, g.srcs, g.dsts, g.weights)
         rng = np.random.default_rng(5)

@@ -404,6 +404,7 @@ gas_status gas_batch_create(int32_t device, void *stream, gas_batch **out) {
     delete b;
     return st;
   }
+  gas::internal::core_keep_csr_perm(b->core, true);
   b->device = device;
   b->stream = (cudaStream_t)stream;
   cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
@@ -455,15 +456,11 @@ gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
   for (int32_t v = 0; v < nVertices; ++v)
     b->maxOutDeg = std::max(b->maxOutDeg, (*g.hOutOff)[(size_t)v + 1] - (*g.hOutOff)[v]);
   st = build_units(b, g, b->chunk);
-  if (st || !weights || nEdges == 0) return st;
-  // weights in CSR order for push rounds (stable by source, as the CSR)
-  std::vector<int32_t> off, wcsr;
-  gas::internal::build_adjacency(nVertices, nEdges, srcs, weights, off, wcsr, nullptr);
-  cudaError_t e = cudaMalloc(&b->weightsOut, sizeof(int32_t) * (size_t)nEdges);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(b->weightsOut, wcsr.data(), sizeof(int32_t) * (size_t)nEdges,
-                   cudaMemcpyHostToDevice);
-  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch CSR weights");
+  if (st == GAS_OK && weights && nEdges > 0)  // weights in CSR order for push rounds
+    st = gas::internal::core_permute_csr(b->core, weights, &b->weightsOut);
+  gas::internal::core_keep_csr_perm(b->core, false);  // the permutation is not needed after this
+  gas::internal::core_keep_csr_perm(b->core, true);   // (kept again by the next set_graph)
+  return st;
 }
 
 gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocksPerSM,

@@ -122,7 +122,10 @@ struct gas_core_s {
   bool haveGraph = false;
   int32_t nV = 0, nE = 0;
   int32_t edgeBytes = 0, vertexBytes = 0, gatherBytes = 0;
-  std::vector<int32_t> hInOff, hOutOff, cscPerm;
+  std::vector<int32_t> hInOff, hOutOff;
+  uint32_t *cscPerm = nullptr;  // [E] edge index at each CSC position (when EdgeData is not empty)
+  uint32_t *csrPerm = nullptr;  // [E] the same for the CSR, kept on request
+  bool keepCsrPerm = false;
   int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
   void *ed = nullptr;
   void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr, *valt = nullptr;
@@ -184,9 +187,11 @@ void free_graph(gas_core *c) {
                   c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
-                  c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats};
+                  c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats,
+                  c->cscPerm, c->csrPerm};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  c->cscPerm = c->csrPerm = nullptr;
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
   c->retStamp[0] = c->retStamp[1] = nullptr;
@@ -277,6 +282,38 @@ gas_status check_device_error(gas_core *c) {
 
 namespace gas {
 namespace internal {
+void core_keep_csr_perm(gas_core_s *c, bool keep) {
+  c->keepCsrPerm = keep;
+  if (!keep && c->csrPerm) {
+    cudaFree(c->csrPerm);
+    c->csrPerm = nullptr;
+  }
+}
+
+gas_status core_permute_csr(gas_core_s *c, const int32_t *hostVals, int32_t **devOut) {
+  *devOut = nullptr;
+  if (!c || !c->haveGraph || !c->csrPerm) return fail(GAS_ERR_STATE, "no CSR permutation kept");
+  const size_t n = (size_t)std::max(c->nE, 1);
+  int32_t *tmp = nullptr, *out = nullptr;
+  cudaError_t e = cudaMalloc(&tmp, 4 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&out, 4 * n);
+  if (e == cudaSuccess && c->nE > 0)
+    e = cudaMemcpyAsync(tmp, hostVals, 4 * (size_t)c->nE, cudaMemcpyHostToDevice, c->stream);
+  gas_status st = e == cudaSuccess ? device_gather_bytes(c->stream, tmp, c->csrPerm, c->nE, 4, out)
+                                   : cuda_fail(e, "CSR permutation");
+  if (st == GAS_OK) {
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "CSR permutation");
+  }
+  if (tmp) cudaFree(tmp);
+  if (st != GAS_OK) {
+    if (out) cudaFree(out);
+    return st;
+  }
+  *devOut = out;
+  return GAS_OK;
+}
+
 bool core_graph(gas_core_s *c, CoreGraph *out) {
   if (!c || !c->haveGraph) return false;
   out->device = c->device;
@@ -365,28 +402,40 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
     return fail(GAS_ERR_INVALID, "edge data is NULL but EdgeData is not empty");
   if ((long long)nV + nE + 2LL * GAS_GATHER_TILE >= (1LL << 31))
     return fail(GAS_ERR_UNSUPPORTED, "vertices + edges must stay below 2^31 (int32 ids)");
-  for (int32_t i = 0; i < nE; ++i)
-    if ((unsigned)srcs[i] >= (unsigned)nV || (unsigned)dsts[i] >= (unsigned)nV)
-      return fail(GAS_ERR_INVALID, "edge %d (%d -> %d) has a vertex id outside [0, %d)", i,
-                  srcs[i], dsts[i], nV);
   gas_status st = set_device(c);
   if (st) return st;
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_graph(c);
 
-  // host CSC (gather) and CSR (scatter), both stable in edge-list order
-  std::vector<int32_t> inSrcH, outDstH;
-  std::vector<int32_t> *perm = edgeBytes > 0 ? &c->cscPerm : nullptr;
-  std::thread tcsr([&] { build_adjacency(nV, nE, srcs, dsts, c->hOutOff, outDstH, nullptr); });
-  build_adjacency(nV, nE, dsts, srcs, c->hInOff, inSrcH, perm);
-  tcsr.join();
-  if (!perm) c->cscPerm.clear();
+  // the edge list on the device: id check, then CSC (gather) and CSR
+  // (scatter) by stable radix sorts (gas_graph_build.cu)
+  int32_t *dS = nullptr, *dD = nullptr;
+  cudaError_t e0 = dalloc(&dS, (size_t)nE);
+  if (e0 == cudaSuccess) e0 = dalloc(&dD, (size_t)nE);
+  if (e0 == cudaSuccess && nE > 0)
+    e0 = cudaMemcpyAsync(dS, srcs, sizeof(int32_t) * nE, cudaMemcpyHostToDevice, c->stream);
+  if (e0 == cudaSuccess && nE > 0)
+    e0 = cudaMemcpyAsync(dD, dsts, sizeof(int32_t) * nE, cudaMemcpyHostToDevice, c->stream);
+  auto drop_list = [&] {
+    if (dS) cudaFree(dS);
+    if (dD) cudaFree(dD);
+  };
+  if (e0 != cudaSuccess) {
+    drop_list();
+    return cuda_fail(e0, "setGraph edge list upload");
+  }
+  long long bad = -1;
+  st = device_first_bad_edge(c->stream, nV, nE, dS, dD, &bad);
+  if (st == GAS_OK && bad >= 0)
+    st = fail(GAS_ERR_INVALID, "edge %lld (%d -> %d) has a vertex id outside [0, %d)", bad,
+              srcs[bad], dsts[bad], nV);
+  if (st) {
+    drop_list();
+    return st;
+  }
 
   c->nV = nV;
   c->nE = nE;
-  c->maxInDeg = 0;
-  for (int32_t v = 0; v < nV; ++v)
-    c->maxInDeg = std::max(c->maxInDeg, c->hInOff[(size_t)v + 1] - c->hInOff[v]);
   c->edgeBytes = edgeBytes;
   c->vertexBytes = vertexBytes;
   c->gatherBytes = gatherBytes;
@@ -402,11 +451,41 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(dalloc(&c->outOff, (size_t)nV + 1));
   A(dalloc(&c->outDst, (size_t)nE));
   if (edgeBytes > 0) A(cudaMalloc(&c->ed, (size_t)edgeBytes * std::max(nE, 1)));
+  if (edgeBytes > 0) A(dalloc(&c->cscPerm, (size_t)nE));
+  if (c->keepCsrPerm) A(dalloc(&c->csrPerm, (size_t)nE));
+  if (e == cudaSuccess) {
+    st = device_build_adjacency(c->stream, nV, nE, dD, dS, c->inOff, c->inSrc, c->cscPerm);
+    if (st == GAS_OK)
+      st = device_build_adjacency(c->stream, nV, nE, dS, dD, c->outOff, c->outDst, c->csrPerm);
+    if (st == GAS_OK && edgeBytes > 0 && nE > 0) {
+      void *dEd = nullptr;
+      A(cudaMalloc(&dEd, (size_t)edgeBytes * nE));
+      A(cudaMemcpyAsync(dEd, edgeData, (size_t)edgeBytes * nE, cudaMemcpyHostToDevice, c->stream));
+      if (e == cudaSuccess) st = device_gather_bytes(c->stream, dEd, c->cscPerm, nE, edgeBytes, c->ed);
+      A(cudaStreamSynchronize(c->stream));
+      if (dEd) cudaFree(dEd);
+    }
+    c->hInOff.resize((size_t)nV + 1);
+    c->hOutOff.resize((size_t)nV + 1);
+    A(cudaMemcpyAsync(c->hInOff.data(), c->inOff, sizeof(int32_t) * ((size_t)nV + 1),
+                      cudaMemcpyDeviceToHost, c->stream));
+    A(cudaMemcpyAsync(c->hOutOff.data(), c->outOff, sizeof(int32_t) * ((size_t)nV + 1),
+                      cudaMemcpyDeviceToHost, c->stream));
+    A(cudaStreamSynchronize(c->stream));
+  }
+  drop_list();
+  if (st != GAS_OK || e != cudaSuccess) {
+    free_graph(c);
+    return st != GAS_OK ? st : cuda_fail(e, "setGraph build");
+  }
   A(cudaMalloc(&c->vd, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->vnew, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->valt, (size_t)vertexBytes * std::max(nV, 1)));
   A(dalloc(&c->retStamp[0], (size_t)nV));
   A(dalloc(&c->retStamp[1], (size_t)nV));
+  c->maxInDeg = 0;
+  for (int32_t v = 0; v < nV; ++v)
+    c->maxInDeg = std::max(c->maxInDeg, c->hInOff[(size_t)v + 1] - c->hInOff[v]);
   // in-degree bins of the dense pass
   std::vector<int32_t> bMid, bSmall, bTiny, chV, chB, chF, chC, chS;
   for (int32_t v = 0; v < nV; ++v) {
@@ -465,26 +544,6 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   if (e != cudaSuccess) {
     free_graph(c);
     return cuda_fail(e, "setGraph device allocation");
-  }
-  A(cudaMemcpyAsync(c->inOff, c->hInOff.data(), sizeof(int32_t) * ((size_t)nV + 1),
-                    cudaMemcpyHostToDevice, c->stream));
-  A(cudaMemcpyAsync(c->outOff, c->hOutOff.data(), sizeof(int32_t) * ((size_t)nV + 1),
-                    cudaMemcpyHostToDevice, c->stream));
-  if (nE > 0) {
-    A(cudaMemcpyAsync(c->inSrc, inSrcH.data(), sizeof(int32_t) * nE, cudaMemcpyHostToDevice,
-                      c->stream));
-    A(cudaMemcpyAsync(c->outDst, outDstH.data(), sizeof(int32_t) * nE, cudaMemcpyHostToDevice,
-                      c->stream));
-  }
-  std::vector<char> edSorted;
-  if (edgeBytes > 0 && nE > 0) {
-    edSorted.resize((size_t)edgeBytes * nE);
-    const char *src = reinterpret_cast<const char *>(edgeData);
-    for (int32_t p = 0; p < nE; ++p)
-      memcpy(&edSorted[(size_t)p * edgeBytes], src + (size_t)c->cscPerm[p] * edgeBytes,
-             edgeBytes);
-    A(cudaMemcpyAsync(c->ed, edSorted.data(), edSorted.size(), cudaMemcpyHostToDevice,
-                      c->stream));
   }
   A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
   for (int k = 0; k < 2; ++k)
@@ -552,16 +611,19 @@ gas_status gas_core_download_edge_data(gas_core *c, void *host) {
   if (!c || !host) return fail(GAS_ERR_INVALID, "download_edge_data: null argument");
   if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
   if (c->edgeBytes == 0 || c->nE == 0) return GAS_OK;
-  std::vector<char> tmp((size_t)c->edgeBytes * c->nE);
-  cudaError_t e = cudaMemcpyAsync(tmp.data(), c->ed, tmp.size(), cudaMemcpyDeviceToHost,
-                                  c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  // back to edge-list order on the device, then one copy
+  void *tmp = nullptr;
+  const size_t bytes = (size_t)c->edgeBytes * c->nE;
+  cudaError_t e = cudaMalloc(&tmp, bytes);
   if (e != cudaSuccess) return cuda_fail(e, "edge data download");
-  char *dst = reinterpret_cast<char *>(host);
-  for (int32_t p = 0; p < c->nE; ++p)
-    memcpy(dst + (size_t)c->cscPerm[p] * c->edgeBytes, &tmp[(size_t)p * c->edgeBytes],
-           c->edgeBytes);
-  return GAS_OK;
+  gas_status st = device_scatter_bytes(c->stream, c->ed, c->cscPerm, c->nE, c->edgeBytes, tmp);
+  if (st == GAS_OK) {
+    e = cudaMemcpyAsync(host, tmp, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) st = cuda_fail(e, "edge data download");
+  }
+  cudaFree(tmp);
+  return st;
 }
 
 gas_status gas_core_vertex_data(gas_core *c, void **dev) {
