@@ -358,6 +358,39 @@ GAS_API gas_status gas_gen_grid(int32_t rows, int32_t cols, double pDelete, uint
 
 GAS_API void gas_edge_list_free(gas_edge_list *l);
 
+/* ---------------- graph files (graphio.cpp) ----------------------------- */
+/* Replaces loadGraph (graphio.cpp:441-473): the format from the extension
+ * (".edge" SNAP, ".mtx" MatrixMarket coordinate, ".gr" Lonestar binary CSR;
+ * text formats may be gzip-compressed, ".gz", when the library was built
+ * with zlib), the same edge list as the reference loaders: self-loops
+ * dropped, symmetric/skew-symmetric/hermitian MatrixMarket files expanded
+ * to both directions, ids 0-based, vertex count = largest id + 1.  With
+ * wantValues, weights receives the edge values (MatrixMarket values
+ * truncated to int; skew-symmetric reverse edges negated; NULL for
+ * "pattern" files).  Errors return a status instead of exiting; hermitian
+ * files with values are refused (the reference loads their values
+ * misaligned); a .gr file without values loads when no values are asked
+ * for (the reference's own writer produces those).  Release with
+ * gas_edge_list_free. */
+GAS_API gas_status gas_load_graph(const char *path, int32_t wantValues, gas_edge_list *out);
+/* Replaces writeGraph_mtx (graphio.cpp:416-438): "%%MatrixMarket matrix
+ * coordinate Integer general", 1-based ids; values may be NULL. */
+GAS_API gas_status gas_write_graph_mtx(const char *path, int32_t nVertices, int64_t nEdges,
+                                       const int32_t *srcs, const int32_t *dsts,
+                                       const int32_t *values);
+/* Replaces writeGraph_binaryCSR (graphio.cpp:365-413): CSR offsets
+ * (nVertices + 1) and destinations; values may be NULL. */
+GAS_API gas_status gas_write_graph_gr(const char *path, int32_t nVertices, int64_t nEdges,
+                                      const int32_t *offsets, const int32_t *dsts,
+                                      const int32_t *values);
+/* The drivers' result files (bfs.cu:115-119, sssp.cu:85-89,
+ * pagerank.cu:77-81): one "vid value" line per vertex, "%d %d" for int32
+ * values or "%d %f" for float; element i at values + i * strideBytes
+ * (0 = 4, e.g. 8 for PageRank's {rank, numOutEdges}). */
+GAS_API gas_status gas_write_vertex_values(const char *path, int32_t nVertices,
+                                           const void *values, int32_t isFloat,
+                                           int32_t strideBytes);
+
 #ifdef __cplusplus
 }
 #endif

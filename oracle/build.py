@@ -59,9 +59,16 @@ def build_ref(force: bool = False) -> str | None:
     if not force and _newer(REF_LIB, needed + [harness, os.path.join(HERE, "gas_oracle.h")]):
         return REF_LIB
     os.makedirs(REF_OUT_DIR, exist_ok=True)
+    # graphio.cpp unoptimised and without unreachable traps:
+    # loadGraph_binaryCSR (graphio.cpp:274-362) has no return statement;
+    # g++ 13 turns falling off its end into a crash (-O2: stack corruption;
+    # -O0 by default: a trap instruction) whenever a .gr file is read.  This
+    # way it returns an unused garbage value, as older compilers did.
+    gio = os.path.join(REF_OUT_DIR, "graphio.o")
+    subprocess.run(["g++", "-O0", "-fno-unreachable-traps", "-std=c++17", "-fPIC", "-w", "-I", rd, "-c",
+                    os.path.join(rd, "graphio.cpp"), "-o", gio], check=True)
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
-           "-I", rd, "-I", HERE, "-o", REF_LIB, harness,
-           os.path.join(rd, "graphio.cpp"), "-lz"]
+           "-I", rd, "-I", HERE, "-o", REF_LIB, harness, gio, "-lz"]
     subprocess.run(cmd, check=True)
     return REF_LIB
 

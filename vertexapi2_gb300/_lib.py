@@ -114,6 +114,11 @@ SIGNATURES = {
                             _I32, _I32, C.POINTER(EdgeList)]),
     "gas_gen_grid": (_I32, [_I32, _I32, C.c_double, C.c_uint64, _I32, _I32, C.POINTER(EdgeList)]),
     "gas_edge_list_free": (None, [C.POINTER(EdgeList)]),
+    # graph files
+    "gas_load_graph": (_I32, [C.c_char_p, _I32, C.POINTER(EdgeList)]),
+    "gas_write_graph_mtx": (_I32, [C.c_char_p, _I32, C.c_int64, _PI32, _PI32, _PI32]),
+    "gas_write_graph_gr": (_I32, [C.c_char_p, _I32, C.c_int64, _PI32, _PI32, _PI32]),
+    "gas_write_vertex_values": (_I32, [C.c_char_p, _I32, _P, _I32, _I32]),
     # core layer
     "gas_core_create": (_I32, [_I32, _P, C.POINTER(_P)]),
     "gas_core_destroy": (_I32, [_P]),

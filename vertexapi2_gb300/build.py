@@ -37,9 +37,27 @@ def headers() -> list[str]:
             + glob.glob(os.path.join(CSRC, "*.h")))
 
 
+_ZLIB = None
+
+
+def zlib_available() -> bool:
+    """Whether zlib's header and library are present (gzip graph files)."""
+    global _ZLIB
+    if _ZLIB is None:
+        prog = "#include <zlib.h>\nint main() { return gzopen(0, 0) != 0; }\n"
+        try:
+            r = subprocess.run(["g++", "-x", "c++", "-", "-lz", "-o", os.devnull], input=prog,
+                               capture_output=True, text=True, timeout=60)
+            _ZLIB = r.returncode == 0
+        except (OSError, subprocess.SubprocessError):
+            _ZLIB = False
+    return _ZLIB
+
+
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [NVCC] + ARCH + COMMON + extra + ["-c", src, "-o", obj]
+    zl = ["-DGAS_HAVE_ZLIB"] if zlib_available() else []
+    cmd = [NVCC] + ARCH + COMMON + zl + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -57,7 +75,7 @@ def build(force: bool = False, extra: list[str] | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     tmp = LIB + ".tmp"
-    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"] + (["-lz"] if zlib_available() else [])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
