@@ -22,6 +22,7 @@
 #pragma once
 
 #include "dense.cuh"
+#include "edge_scatter.cuh"
 #include "gather.cuh"
 #include "scatter.cuh"
 
@@ -187,6 +188,14 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
           else
             scatter_tile(sa, t, ns, Ts, sm.s);
           __syncthreads();
+        }
+      }
+      if constexpr (ProgramScatterEdges<P>::value) {
+        if (ra.edgeScatter) {
+          // Program::scatter sees the committed vertex data of every vertex
+          if (!grid_barrier(ra.barrier, a.errWord)) break;
+          edge_scatter_vertices<P>(a.scat.vid, ns, a.outOffsets, ra.outDests, ra.csr2csc,
+                                   vdBuf[vcur], const_cast<void *>(a.edgeData));
         }
       }
       if (!grid_barrier(ra.barrier, a.errWord)) break;

@@ -22,7 +22,13 @@
 //     haveGather = false` to make run() skip the gather (as bfs.cu does by
 //     calling gatherApply(false));
 //   * getResults() returns edge data in the caller's original order (the
-//     reference copies CSC-sorted data back, gpugas.h:333-336).
+//     reference copies CSC-sorted data back, gpugas.h:333-336);
+//   * a Program declaring `static constexpr bool scatterEdges = true` (and
+//     a non-empty EdgeData) has scatter(src, dst, edge) called on every
+//     out-edge of the vertices whose apply returned true, by
+//     scatterActivate(true) and by run(), as the reference's CPU engine
+//     does (refgas.h:171-197); otherwise scatter is not called, as in the
+//     reference's GPU engine (gpugas.h:666-668).
 // gatherZero must be usable in device code (constexpr or an integral
 // static const).
 #pragma once
@@ -71,6 +77,7 @@ class EngineGPU {
     vdHost_ = vertexData;
     edHost_ = edgeData;
     const int32_t eb = kEdgeBytes;
+    if (kScatterEdges && !note(gas_core_enable_edge_scatter(core_, 1))) return;
     if (!note(gas_core_set_graph(core_, nVertices, nEdges, edgeListSrcs, edgeListDsts,
                                  eb ? (const void *)edgeData : nullptr, eb,
                                  (int32_t)sizeof(VertexData), (int32_t)sizeof(GatherResult))))
@@ -101,11 +108,13 @@ class EngineGPU {
     note(gas_core_gather_apply(core_, haveGather ? 1 : 0, &launch, this));
   }
 
-  // gpugas.h:669-751.  Program::scatter is not called, as in the
-  // reference's GPU engine (gpugas.h:666-668).
+  // gpugas.h:669-751.  Program::scatter runs only for Programs that opt in
+  // (scatterEdges), after the activation.
   void scatterActivate(bool haveScatter = true) {
-    (void)haveScatter;
-    note(gas_core_scatter_activate(core_));
+    if (!note(gas_core_scatter_activate(core_))) return;
+    if constexpr (kScatterEdges) {
+      if (haveScatter) note(gas_core_edge_scatter(core_, &launchEdgeScatter, this));
+    }
   }
 
   // gpugas.h:754-758
@@ -121,6 +130,24 @@ class EngineGPU {
   // returns the number of rounds executed.
   int32_t runFor(int32_t maxIters) {
     int32_t it = 0;
+    if (kScatterEdges && persistent_) {
+      const gas_status st =
+          gas_core_run_persistent(core_, maxIters, ProgramHaveGather<Program>::value ? 1 : 0,
+                                  &launchRun, &launch, this, &it);
+      if (st != GAS_ERR_UNSUPPORTED) {
+        note(st);
+        return it;
+      }
+    }
+    if (kScatterEdges) {  // the rounds one call at a time (refgas.h:216-224)
+      while ((maxIters <= 0 || it < maxIters) && countActive() > 0 && status_ == GAS_OK) {
+        gatherApply(ProgramHaveGather<Program>::value);
+        scatterActivate(true);
+        nextIter();
+        ++it;
+      }
+      return it;
+    }
     note(gas_core_run_persistent(core_, maxIters, ProgramHaveGather<Program>::value ? 1 : 0,
                                  persistent_ ? &launchRun : nullptr, &launch, this, &it));
     return it;
@@ -146,6 +173,8 @@ class EngineGPU {
  private:
   static constexpr int32_t kEdgeBytes =
       std::is_empty<EdgeData>::value ? 0 : (int32_t)sizeof(EdgeData);
+  static constexpr bool kScatterEdges =
+      detail::ProgramScatterEdges<Program>::value && kEdgeBytes > 0;
 
   bool note(gas_status s) {
     status_ = s;
@@ -191,8 +220,22 @@ class EngineGPU {
     return e == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
   }
 
+  static gas_status launchEdgeScatter(void *user, const gas_edge_scatter_args *a, void *stream) {
+    EngineGPU *self = static_cast<EngineGPU *>(user);
+    if (self->scatterGrid_ == 0) {
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      self->scatterGrid_ = 4 * (sms > 0 ? sms : 1);
+    }
+    if constexpr (kScatterEdges)
+      detail::edge_scatter_kernel<Program><<<self->scatterGrid_, 256, 0, (cudaStream_t)stream>>>(*a);
+    return cudaGetLastError() == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
+  }
+
   gas_core *core_ = nullptr;
   gas_status status_ = GAS_OK;
+  int scatterGrid_ = 0;
   bool persistent_ = true;
   int runGrid_ = 0;
   int runBlocksPerSM_ = 0;

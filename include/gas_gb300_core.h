@@ -141,7 +141,23 @@ typedef struct {
   unsigned *chunkArrive;      /* [2][nChunkVertices] arrival counters        */
   void *chunkVal;             /* [nChunks] GatherResult partials             */
   unsigned *chunkFlags;       /* [nChunks] has | act << 1                    */
+  /* Program::scatter over the out-edges of each round's ret vertices
+   * (gas_core_enable_edge_scatter); dense rounds are off then */
+  int32_t edgeScatter;
+  const int32_t *csr2csc;     /* [E] CSC position of the edge at each CSR position */
 } gas_run_args;
+
+/* The vertices whose apply returned true in the round just scattered, for
+ * a Program's scatter over their out-edges (edge data in CSC order). */
+typedef struct {
+  const int32_t *vid;                 /* [count] vertex ids                   */
+  const unsigned long long *count;    /* device: count << 32 | out-degree sum */
+  const int32_t *outOffsets;          /* CSR                                  */
+  const int32_t *outDests;
+  const int32_t *csr2csc;             /* [E] CSC position of each CSR edge    */
+  void *vertexData;
+  void *edgeData;                     /* CSC order                            */
+} gas_edge_scatter_args;
 
 typedef struct gas_core_s gas_core;
 
@@ -152,6 +168,9 @@ typedef gas_status (*gas_gather_launch_fn)(void *user, const gas_gather_args *ar
  * Returns GAS_ERR_UNSUPPORTED when it cannot be launched co-resident; the
  * core then falls back to one launch per phase. */
 typedef gas_status (*gas_run_launch_fn)(void *user, const gas_run_args *args, void *stream);
+/* Launches the caller's Program::scatter kernel. */
+typedef gas_status (*gas_edge_scatter_fn)(void *user, const gas_edge_scatter_args *args,
+                                          void *stream);
 
 GAS_API gas_status gas_core_create(int32_t device, void *stream, gas_core **out);
 GAS_API gas_status gas_core_destroy(gas_core *c);
@@ -214,6 +233,17 @@ GAS_API gas_status gas_core_kernel_times(gas_core *c, float *gatherMs, float *sc
                                          int32_t *gatherLaunches, int32_t *scatterLaunches);
 /* Waits for queued work and reports device-side errors. */
 GAS_API gas_status gas_core_sync(gas_core *c);
+
+/* Program::scatter(src, dst, edge) for every out-edge of the vertices whose
+ * apply returned true, after their activation, as the reference's CPU
+ * engine does (refgas.h:171-197); its GPU engine never calls it
+ * (gpugas.h:666-668).  Enable before gas_core_set_graph (the graph then
+ * keeps the CSR -> CSC edge map; getResults returns the edge data in the
+ * caller's order).  run() then uses list rounds only. */
+GAS_API gas_status gas_core_enable_edge_scatter(gas_core *c, int32_t on);
+/* After gas_core_scatter_activate and before gas_core_next_iter: hands
+ * the round's vertices to the caller's scatter kernel. */
+GAS_API gas_status gas_core_edge_scatter(gas_core *c, gas_edge_scatter_fn launch, void *user);
 
 #ifdef __cplusplus
 }

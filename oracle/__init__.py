@@ -38,6 +38,7 @@ _SIGS = {
     "run_cc": [C.c_int32, C.c_int32, _PI, _PI, _PI, _PS],
     "run_pagerank_f32": [C.c_int32, C.c_int32, _PI, _PI, C.c_int32, C.POINTER(C.c_float), _PS],
     "run_pagerank_f64": [C.c_int32, C.c_int32, _PI, _PI, C.c_int32, C.POINTER(C.c_double), _PS],
+    "run_sssp_visits": [C.c_int32, C.c_int32, _PI, _PI, _PI, C.c_int32, _PI, _PI, _PI, _PS],
     "run_ppr_f32": [C.c_int32, C.c_int32, _PI, _PI, C.c_int32, C.c_float, C.c_int32,
                     C.POINTER(C.c_float), _PS],
     "run_ppr_f64": [C.c_int32, C.c_int32, _PI, _PI, C.c_int32, C.c_double, C.c_int32,
@@ -112,6 +113,19 @@ class Engine:
         st = self._call("run_sssp", n, len(s), ps, pd, w.ctypes.data_as(_PI), source,
                         out.ctypes.data_as(_PI), cap=stats_cap)
         return out[:n], st
+
+    def sssp_visits(self, n, srcs, dsts, weights, source, stats_cap=0):
+        """SSSP whose Program::scatter counts visits per edge and records the
+        source distance: (dist, visits, last), edge arrays in edge order."""
+        s, d, ps, pd = self._edges(srcs, dsts)
+        w = np.ascontiguousarray(weights, dtype=np.int32)
+        dist = np.zeros(max(n, 1), dtype=np.int32)
+        vis = np.zeros(max(len(s), 1), dtype=np.int32)
+        last = np.zeros(max(len(s), 1), dtype=np.int32)
+        p = lambda a: a.ctypes.data_as(_PI)
+        st = self._call("run_sssp_visits", n, len(s), ps, pd, p(w), source, p(dist), p(vis), p(last),
+                        cap=stats_cap)
+        return dist[:n], vis[:len(s)], last[:len(s)], st
 
     def cc(self, n, srcs, dsts, stats_cap=0):
         s, d, ps, pd = self._edges(srcs, dsts)

@@ -215,6 +215,32 @@ static inline int sssp_apply(int32_t *cur, int32_t d)
 #undef ORA_APPLY
 #undef ORA_HAS_ED
 
+/* SSSP whose scatter writes its edge (not a reference program): a visit
+ * count and the source's distance at the visit -- exercises the engine's
+ * call of Program::scatter (refgas.h:171-197). */
+typedef struct { int32_t w, visits, last; } visit_ed;
+#define ORA_FN(x) sssp_visits_##x
+#define ORA_VD int32_t
+#define ORA_ED visit_ed
+#define ORA_GR int32_t
+#define ORA_GZERO SSSP_GZERO
+#define ORA_GATHER_MAP(d, s, e) ((void)(d), *(s) + (e)->w)
+#define ORA_GATHER_REDUCE(a, b) imin32(a, b)
+#define ORA_APPLY(v, g, it, e) ((void)(it), (void)(e), sssp_apply(v, g))
+#define ORA_HAS_ED 1
+#define ORA_SCATTER(s, d, e) ((void)(d), (e)->visits += 1, (e)->last = *(s))
+#include "gas_oracle_engine.inc"
+#undef ORA_FN
+#undef ORA_VD
+#undef ORA_ED
+#undef ORA_GR
+#undef ORA_GZERO
+#undef ORA_GATHER_MAP
+#undef ORA_GATHER_REDUCE
+#undef ORA_APPLY
+#undef ORA_HAS_ED
+#undef ORA_SCATTER
+
 /* Connected components, connected_component.cu:25-63 */
 #define ORA_FN(x) cc_##x
 #define ORA_VD int32_t
@@ -368,6 +394,31 @@ int ora_run_sssp(int32_t nV, int32_t nE, const int32_t *srcs,
   ora_set_active(&e, 0, nV);
   sssp_run(&e, dist, weights, 0, st);
   ora_engine_free(&e);
+  return 0;
+}
+
+/* The scatter-writing SSSP, driven as sssp.cu:67-82: edge data {w,
+ * visits, last} in edge-list order (visits/last start at 0). */
+int ora_run_sssp_visits(int32_t nV, int32_t nE, const int32_t *srcs,
+                        const int32_t *dsts, const int32_t *weights, int32_t source,
+                        int32_t *dist, int32_t *visits, int32_t *last, ora_stats *st)
+{
+  if (ora_check_edges(nV, nE, srcs, dsts) || !dist || !visits || !last) return 1;
+  if (source < 0 || source >= nV || (nE > 0 && !weights)) return 1;
+  for (int32_t i = 0; i < nV; ++i) dist[i] = SSSP_GZERO;
+  dist[source] = 0;
+  visit_ed *ed = (visit_ed *)calloc((size_t)(nE > 0 ? nE : 1), sizeof(visit_ed));
+  for (int32_t i = 0; i < nE; ++i) ed[i].w = weights[i];
+  ora_engine e;
+  ora_engine_init(&e, nV, nE, srcs, dsts);
+  ora_set_active(&e, 0, nV);
+  sssp_visits_run(&e, dist, ed, 0, st);
+  ora_engine_free(&e);
+  for (int32_t i = 0; i < nE; ++i) {
+    visits[i] = ed[i].visits;
+    last[i] = ed[i].last;
+  }
+  free(ed);
   return 0;
 }
 

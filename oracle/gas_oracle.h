@@ -65,6 +65,12 @@ int ora_run_sssp(int32_t nV, int32_t nE, const int32_t *srcs,
                  const int32_t *dsts, const int32_t *weights, int32_t source,
                  int32_t *dist, ora_stats *stats);
 
+/* SSSP whose Program::scatter writes each visited edge (visits += 1,
+ * last = source distance): the engine's scatter call (refgas.h:171-197). */
+int ora_run_sssp_visits(int32_t nV, int32_t nE, const int32_t *srcs,
+                        const int32_t *dsts, const int32_t *weights, int32_t source,
+                        int32_t *dist, int32_t *visits, int32_t *last, ora_stats *stats);
+
 int ora_run_cc(int32_t nV, int32_t nE, const int32_t *srcs,
                const int32_t *dsts, int32_t *label, ora_stats *stats);
 

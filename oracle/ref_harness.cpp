@@ -66,6 +66,26 @@ struct SSSP {
   static void scatter(const VertexData *, const VertexData *, EdgeData *) {}
 };
 
+// An SSSP whose scatter writes its edge (not a reference program): a visit
+// count and the source's distance, through refgas.h's own scatter call.
+struct SSSPVisits {
+  typedef int VertexData;
+  struct EdgeData { int w, visits, last; };
+  typedef int GatherResult;
+  static const int gatherZero = INT_MAX - 100000;
+  static int gatherReduce(const int &l, const int &r) { return min(l, r); }
+  static int gatherMap(const VertexData *, const VertexData *s, const EdgeData *e) { return *s + e->w; }
+  static bool apply(VertexData *cur, GatherResult d) {
+    bool changed = d < *cur;
+    *cur = min(*cur, d);
+    return changed;
+  }
+  static void scatter(const VertexData *src, const VertexData *, EdgeData *e) {
+    e->visits += 1;
+    e->last = *src;
+  }
+};
+
 struct CC {
   typedef int VertexData;
   struct EdgeData {};
@@ -212,6 +232,26 @@ int ref_run_pagerank_f32(int32_t nV, int32_t nE, const int32_t *s, const int32_t
 int ref_run_pagerank_f64(int32_t nV, int32_t nE, const int32_t *s, const int32_t *d,
                          int32_t max_iters, double *rank, ora_stats *st) {
   return pr_run<double>(nV, nE, s, d, max_iters, rank, st);
+}
+
+int ref_run_sssp_visits(int32_t nV, int32_t nE, const int32_t *srcs, const int32_t *dsts,
+                        const int32_t *w, int32_t source, int32_t *dist, int32_t *visits,
+                        int32_t *last, ora_stats *st) {
+  if (bad_edges(nV, nE, srcs, dsts) || source < 0 || source >= nV) return 1;
+  std::vector<int> vd(nV, SSSPVisits::gatherZero);
+  vd[source] = 0;
+  std::vector<SSSPVisits::EdgeData> ed(nE > 0 ? nE : 1);
+  for (int i = 0; i < nE; ++i) ed[i] = {w[i], 0, 0};
+  GASEngineRef<SSSPVisits> e;
+  e.setGraph(nV, vd.data(), nE, ed.data(), srcs, dsts);
+  e.setActive(0, nV);
+  drive(e, 0, st, false);
+  for (int i = 0; i < nV; ++i) dist[i] = vd[i];
+  for (int i = 0; i < nE; ++i) {
+    visits[i] = ed[i].visits;
+    last[i] = ed[i].last;
+  }
+  return 0;
 }
 
 // graphio.cpp:441-473 loadGraph; arrays are malloc'd, free with ref_free.

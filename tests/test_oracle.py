@@ -101,3 +101,21 @@ def test_port_matches_reference_engine(port, seed):
         b, sb = ref.pagerank(nv, s, d, max_iters=50, fp64=True)
         assert np.allclose(a, b, rtol=1e-12, atol=1e-12)
         assert sa["iterations"] == sb["iterations"]
+
+
+def test_scatter_program_port_matches_reference():
+    """A Program whose scatter writes its edge (visit count, source
+    distance): the restatement calls Program::scatter as refgas.h does."""
+    import oracle
+    from vertexapi2_gb300 import graphs
+    ref = oracle.ref()
+    if ref is None:
+        pytest.skip("reference engine not built")
+    port = oracle.port()
+    for seed in range(4):
+        g = graphs.rmat(9, 8, seed=70 + seed, weights=(1, 30))
+        a = port.sssp_visits(g.n_vertices, g.srcs, g.dsts, g.weights, seed)
+        b = ref.sssp_visits(g.n_vertices, g.srcs, g.dsts, g.weights, seed)
+        for x, y in zip(a[:3], b[:3]):
+            assert np.array_equal(x, y)
+        assert a[1].sum() > 0

@@ -144,6 +144,8 @@ SIGNATURES = {
     "gas_core_set_profiling": (_I32, [_P, _I32]),
     "gas_core_set_dense_policy": (_I32, [_P, _I32]),
     "gas_core_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
+    "gas_core_enable_edge_scatter": (_I32, [_P, _I32]),
+    "gas_core_edge_scatter": (_I32, [_P, _P, _P]),
 }
 
 _lib = None

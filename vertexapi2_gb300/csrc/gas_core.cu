@@ -126,6 +126,9 @@ struct gas_core_s {
   uint32_t *cscPerm = nullptr;  // [E] edge index at each CSC position (when EdgeData is not empty)
   uint32_t *csrPerm = nullptr;  // [E] the same for the CSR, kept on request
   bool keepCsrPerm = false;
+  int32_t *csr2csc = nullptr;   // [E] CSC position of each CSR edge (Program::scatter)
+  bool edgeScatterOn = false;   // keep csr2csc and run scatter-capable rounds
+  bool edgeScatterReady = false;  // a scatter list awaits the Program's scatter
   int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
   void *ed = nullptr;
   void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr, *valt = nullptr;
@@ -188,10 +191,11 @@ void free_graph(gas_core *c) {
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
                   c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats,
-                  c->cscPerm, c->csrPerm};
+                  c->cscPerm, c->csrPerm, c->csr2csc};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->cscPerm = c->csrPerm = nullptr;
+  c->csr2csc = nullptr;
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
   c->retStamp[0] = c->retStamp[1] = nullptr;
@@ -452,11 +456,15 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(dalloc(&c->outDst, (size_t)nE));
   if (edgeBytes > 0) A(cudaMalloc(&c->ed, (size_t)edgeBytes * std::max(nE, 1)));
   if (edgeBytes > 0) A(dalloc(&c->cscPerm, (size_t)nE));
-  if (c->keepCsrPerm) A(dalloc(&c->csrPerm, (size_t)nE));
+  const bool edgeMap = c->edgeScatterOn && edgeBytes > 0;
+  if (c->keepCsrPerm || edgeMap) A(dalloc(&c->csrPerm, (size_t)nE));
+  if (edgeMap) A(dalloc(&c->csr2csc, (size_t)nE));
   if (e == cudaSuccess) {
     st = device_build_adjacency(c->stream, nV, nE, dD, dS, c->inOff, c->inSrc, c->cscPerm);
     if (st == GAS_OK)
       st = device_build_adjacency(c->stream, nV, nE, dS, dD, c->outOff, c->outDst, c->csrPerm);
+    if (st == GAS_OK && edgeMap)
+      st = device_csr_to_csc(c->stream, nE, c->cscPerm, c->csrPerm, c->csr2csc);
     if (st == GAS_OK && edgeBytes > 0 && nE > 0) {
       void *dEd = nullptr;
       A(cudaMalloc(&dEd, (size_t)edgeBytes * nE));
@@ -477,6 +485,10 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   if (st != GAS_OK || e != cudaSuccess) {
     free_graph(c);
     return st != GAS_OK ? st : cuda_fail(e, "setGraph build");
+  }
+  if (edgeMap && !c->keepCsrPerm) {  // only the composed map is needed
+    cudaFree(c->csrPerm);
+    c->csrPerm = nullptr;
   }
   A(cudaMalloc(&c->vd, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->vnew, (size_t)vertexBytes * std::max(nV, 1)));
@@ -793,6 +805,7 @@ gas_status gas_core_scatter_activate(gas_core *c) {
   c->pendingCommit = false;
   c->haveScatList = false;
   c->countValid = false;
+  c->edgeScatterReady = true;
   ++c->round;
   return GAS_OK;
 }
@@ -804,6 +817,7 @@ gas_status gas_core_next_iter(gas_core *c) {
   c->sidx ^= 1;
   c->rangeMode = false;
   c->countValid = false;
+  c->edgeScatterReady = false;
   return GAS_OK;
 }
 
@@ -978,12 +992,17 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.chunkVal = c->chunkVal;
   ra.chunkFlags = c->chunkFlags;
   ra.denseCnt = &c->ctl->dense[0][0];
-  ra.denseAlpha = c->denseAlpha;
-  ra.allActive = (c->rangeMode && c->rstart == 0 && c->rcount == c->nV && c->denseAlpha > 0) ? 1 : 0;
+  ra.edgeScatter = c->csr2csc ? 1 : 0;
+  ra.csr2csc = c->csr2csc;
+  ra.denseAlpha = ra.edgeScatter ? 0 : c->denseAlpha;  // Program::scatter walks list rounds
+  ra.allActive =
+      (c->rangeMode && c->rstart == 0 && c->rcount == c->nV && ra.denseAlpha > 0) ? 1 : 0;
   ra.vcurOut = &c->ctl->vcur;
 
   cudaEventRecord(c->t0, c->stream);
   st = runLaunch(user, &ra, (void *)c->stream);
+  if (st == GAS_ERR_UNSUPPORTED && ra.edgeScatter)  // the caller steps the rounds itself
+    return fail(GAS_ERR_UNSUPPORTED, "persistent run unavailable");
   if (st == GAS_ERR_UNSUPPORTED) return gas_core_run(c, maxIters, haveGather, launch, user, iterations);
   if (st) return st;
   e = cudaGetLastError();
@@ -1093,6 +1112,35 @@ gas_status gas_core_kernel_times(gas_core *c, float *gatherMs, float *scatterMs,
   if (gatherLaunches) *gatherLaunches = c->gatherLaunches;
   if (scatterLaunches) *scatterLaunches = c->scatterLaunches;
   return GAS_OK;
+}
+
+gas_status gas_core_enable_edge_scatter(gas_core *c, int32_t on) {
+  if (!c) return fail(GAS_ERR_INVALID, "enable_edge_scatter: engine is NULL");
+  c->edgeScatterOn = on != 0;
+  return GAS_OK;
+}
+
+gas_status gas_core_edge_scatter(gas_core *c, gas_edge_scatter_fn launch, void *user) {
+  if (!c || !launch) return fail(GAS_ERR_INVALID, "edge_scatter: null argument");
+  if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (!c->csr2csc)
+    return fail(GAS_ERR_STATE, "edge scatter needs gas_core_enable_edge_scatter before setGraph "
+                               "and non-empty EdgeData");
+  if (!c->edgeScatterReady) return fail(GAS_ERR_STATE, "edge scatter needs a scatterActivate first");
+  gas_status st = set_device(c);
+  if (st) return st;
+  gas_edge_scatter_args a;
+  a.vid = c->svid[c->sidx];
+  a.count = &c->ctl->s[c->sidx].cnt;
+  a.outOffsets = c->outOff;
+  a.outDests = c->outDst;
+  a.csr2csc = c->csr2csc;
+  a.vertexData = c->vd;
+  a.edgeData = c->ed;
+  st = launch(user, &a, (void *)c->stream);
+  if (st) return st;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "edge scatter launch");
 }
 
 gas_status gas_core_sync(gas_core *c) {

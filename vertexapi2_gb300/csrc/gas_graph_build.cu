@@ -209,6 +209,18 @@ __global__ void check_ids_kernel(const int32_t *a, const int32_t *b, long long n
       atomicMin(firstBad, (unsigned long long)i);
 }
 
+__global__ void invert_kernel(const uint32_t *perm, long long n, uint32_t *inv) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x)
+    inv[perm[p]] = (uint32_t)p;
+}
+
+__global__ void compose_kernel(const uint32_t *inv, const uint32_t *perm, long long n, int32_t *out) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    out[q] = (int32_t)inv[perm[q]];
+}
+
 int grid_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 16)); }
 
 }  // namespace
@@ -287,6 +299,20 @@ gas_status device_build_adjacency(cudaStream_t s, int32_t nV, int32_t nE, const 
   cudaFreeAsync(hist, s);
   if (st) return st;
   return e == cudaSuccess ? GAS_OK : cuda_fail(e, "graph build");
+}
+
+gas_status device_csr_to_csc(cudaStream_t s, int32_t n, const uint32_t *cscPerm,
+                             const uint32_t *csrPerm, int32_t *out) {
+  if (n <= 0) return GAS_OK;
+  uint32_t *inv = nullptr;
+  cudaError_t e = cudaMallocAsync(&inv, sizeof(uint32_t) * n, s);
+  if (e == cudaSuccess) {
+    invert_kernel<<<grid_for(n), 256, 0, s>>>(cscPerm, n, inv);
+    compose_kernel<<<grid_for(n), 256, 0, s>>>(inv, csrPerm, n, out);
+    e = cudaGetLastError();
+    cudaFreeAsync(inv, s);
+  }
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "CSR to CSC edge map");
 }
 
 gas_status device_gather_bytes(cudaStream_t s, const void *dIn, const uint32_t *dPerm, int32_t n,

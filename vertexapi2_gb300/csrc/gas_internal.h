@@ -31,6 +31,9 @@ gas_status device_build_adjacency(cudaStream_t s, int32_t nV, int32_t nE, const 
 // Index of the first edge with an id outside [0, nV), or -1 (waits).
 gas_status device_first_bad_edge(cudaStream_t s, int32_t nV, int32_t nE, const int32_t *dSrcs,
                                  const int32_t *dDsts, long long *firstBad);
+// out[q] = CSC position of the edge at CSR position q.
+gas_status device_csr_to_csc(cudaStream_t s, int32_t n, const uint32_t *cscPerm,
+                             const uint32_t *csrPerm, int32_t *out);
 // out[p] = in[perm[p]] / out[perm[p]] = in[p] for n elements of `bytes`.
 gas_status device_gather_bytes(cudaStream_t s, const void *dIn, const uint32_t *dPerm, int32_t n,
                                int32_t bytes, void *dOut);
