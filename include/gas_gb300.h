@@ -328,6 +328,15 @@ GAS_API const char *gas_status_string(gas_status s);
 GAS_API const char *gas_last_error(void);
 /* 1 when a CUDA device with compute capability 10.3 is present. */
 GAS_API int32_t gas_device_supported(int32_t device);
+/* Failure path of a stalled round, without a fault (no reference
+ * counterpart; the reference's waits are host-side): the grid barrier of
+ * the persistent kernels and the look-back wait of the gather tiles each
+ * wait on a partner that never arrives, give up at their spin limits
+ * (seconds), and report GAS_ERR_TIMEOUT in *barrierStatus /
+ * *lookbackStatus; the device stays usable.  *seconds (may be NULL)
+ * receives the wall time of both. */
+GAS_API gas_status gas_selftest_bounded_waits(int32_t device, gas_status *barrierStatus,
+                                              gas_status *lookbackStatus, float *seconds);
 
 /* ---------------- synthetic graph generators (host) --------------------- */
 /* Edge lists are allocated by the library; release with gas_edge_list_free.

@@ -7,8 +7,9 @@
 // nothing depends on co-residency (unlike the persistent kernels, whose
 // grid barriers need every block resident).
 //
-// BFS / SSSP reuse the batched units of batch.cuh: round r is
-//   batch_round_kernel(r)  resets, push or pull pass, changed count
+// BFS / SSSP reuse the batched units of batch.cuh (the (vertex, query) pair
+// frontier and SSSP distance buckets included): round r is
+//   batch_round_kernel(r)  bounds, resets, pair / push / pull pass, count
 //   batch_tail_kernel(r)   end test (sets done, rounds) or compaction
 // and both return at once when the batch is done, so the host may queue
 // rounds ahead of the end test.
@@ -39,17 +40,35 @@ template <int W, int KIND>
 __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int r,
                                                           const unsigned *done) {
   if (ld_acquire(done)) return;
+  __shared__ int32_t sBound[32 * W];
+  __shared__ unsigned sNear[W];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const size_t maskWords = (size_t)a.nVertices * W;
   const int rc = r % 3, rn = (r + 1) % 3;
+  const bool buckets = KIND == kBatchSSSP && a.delta > 0;
+  const BatchBucket bk{buckets ? sBound : nullptr, buckets ? sNear : nullptr};
+  if (buckets) {  // this round's bounds (as in batch_run_kernel)
+    const int32_t *tPrev = (r & 1) ? a.thresh[1] : a.thresh[0];
+    int32_t *tNext = (r & 1) ? a.thresh[0] : a.thresh[1];
+    const unsigned *nPrev = a.nearFlag[(r + 2) % 3];
+    for (int q = threadIdx.x; q < 32 * W; q += blockDim.x) {
+      int32_t t = __ldcg(tPrev + q);
+      if (r > 0 && !((__ldcg(nPrev + q / 32) >> (q % 32)) & 1u)) t += a.delta;
+      sBound[q] = t;
+      if (blockIdx.x == 0) tNext[q] = t;
+    }
+    if (threadIdx.x < W) sNear[threadIdx.x] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x < W) a.nearFlag[rn][threadIdx.x] = 0u;
+    __syncthreads();
+  }
   const unsigned *cur = a.mask[rc];
   unsigned *nxt = a.mask[rn];
   unsigned *clr = a.mask[(r + 2) % 3];
   const unsigned long long lc = a.listCnt[rc];
   const long long nList = (long long)(lc >> 32);
   const long long eOut = (long long)(lc & 0xffffffffull);
-  const bool push = eOut * a.alpha <= (long long)a.nEdges;
+  const bool push = a.pairMode || buckets || eOut * a.alpha <= (long long)a.nEdges;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.cnt[rn] = 0ull;
     a.listCnt[(r + 2) % 3] = 0ull;
@@ -58,16 +77,30 @@ __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int
        i += (size_t)gridDim.x * blockDim.x)
     clr[i] = 0u;
   unsigned long long changed = 0ull;
-  if (push) {
+  if (a.pairMode) {
+    const uint32_t *pc = a.pairs[rc];
+    uint32_t *pn = a.pairs[rn];
+    const long long threads = (long long)gridDim.x * blockDim.x;
+    for (long long base = gw * 32; base < nList; base += threads) {
+      const long long i = base + (threadIdx.x & 31);
+      const bool valid = i < nList;
+      batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, nxt, pn, a.listCnt + rn,
+                               changed, bk);
+    }
+  } else if (push) {
     for (long long i = gw; i < nList; i += warps)
       batch_push_unit<W, KIND>(a, a.list[rc][i], a.listC[rc][i], r, cur, nxt, a.list[rn],
-                               a.listC[rn], a.listCnt + rn, changed);
+                               a.listC[rn], a.listCnt + rn, changed, bk);
   } else {
     for (long long u = gw; u < a.nUnits; u += warps)
       batch_unit<W, KIND>(a, (int)u, r, cur, nxt, changed);
   }
   changed = warp_sum_u64(changed);
   if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + rc, changed);
+  if (buckets) {
+    __syncthreads();
+    if (threadIdx.x < W && sNear[threadIdx.x]) atomicOr(a.nearFlag[rc] + threadIdx.x, sNear[threadIdx.x]);
+  }
 }
 
 // End of round r: no change -> done (rounds = r, as the persistent kernel
@@ -84,7 +117,8 @@ __global__ void __launch_bounds__(256) batch_tail_kernel(const BatchArgs a, int 
     return;
   }
   const unsigned long long lc = a.listCnt[r % 3];
-  const bool push = (long long)(lc & 0xffffffffull) * a.alpha <= (long long)a.nEdges;
+  const bool push = a.pairMode || a.delta > 0 ||
+                    (long long)(lc & 0xffffffffull) * a.alpha <= (long long)a.nEdges;
   if (push) return;
   const int rn = (r + 1) % 3;
   batch_compact<W>(a, a.mask[rn], a.list[rn], a.listC[rn], a.listCnt + rn);

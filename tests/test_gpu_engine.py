@@ -348,3 +348,16 @@ def test_device_graph_build_order(gpu, port, nv, ne, seed):
         e.get_results()
     assert np.array_equal(ed, w)
     assert np.array_equal(vd, port.sssp(nv, s, d, w, 0)[0])
+
+
+def test_bounded_waits_report_timeouts_and_device_recovers(gpu, port):
+    """A grid barrier and a look-back wait whose partners never arrive give
+    up at their spin limits with GAS_ERR_TIMEOUT; the next run is normal."""
+    import ctypes as C
+    b, l, t = C.c_int32(), C.c_int32(), C.c_float()
+    assert gpu.gas_selftest_bounded_waits(0, C.byref(b), C.byref(l), C.byref(t)) == 0
+    assert b.value == 4 and l.value == 4  # GAS_ERR_TIMEOUT
+    assert 0.0 < t.value < 60.0
+    g = graphs.rmat(8, 8, seed=9, symmetrize=True)
+    depth, _, _ = gpu_bfs(g.n_vertices, g.srcs, g.dsts, 0)
+    assert np.array_equal(depth, port.bfs(g.n_vertices, g.srcs, g.dsts, 0)[0])

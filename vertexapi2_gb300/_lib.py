@@ -109,6 +109,7 @@ SIGNATURES = {
     "gas_status_string": (C.c_char_p, [_I32]),
     "gas_last_error": (C.c_char_p, []),
     "gas_device_supported": (_I32, [_I32]),
+    "gas_selftest_bounded_waits": (_I32, [_I32, _PI32, _PI32, C.POINTER(C.c_float)]),
     # generators
     "gas_gen_rmat": (_I32, [_I32, _I32, C.c_double, C.c_double, C.c_double, C.c_uint64, _I32,
                             _I32, _I32, C.POINTER(EdgeList)]),

@@ -79,7 +79,8 @@ struct ServeGraph {
   int32_t *pprMem = nullptr;      // unitV | unitBeg | unitLen | unitSlot | slotFirst | slotCount | slotHub
   int32_t pprUnits = 0, pprSlots = 0, pprHubs = 0;
   bool weighted = false;
-  int blocksRound[2] = {0, 0};   // BFS/SSSP round grid per W class
+  int32_t maxOutDeg = 0;         // pair frontier when small (lattice-like graphs)
+  int32_t maxWeight = 0;
   int64_t bytes = 0;
 };
 
@@ -121,6 +122,8 @@ struct Batch {
   Ctl *ctl = nullptr;              // inside `state`
   gas::detail::BatchArgs ba;
   gas::detail::PprArgs pa;
+  bool pairs = false;             // (vertex, query) pair frontier
+  int32_t delta = 0;              // SSSP distance buckets
   int roundsIssued = 0;
   int chunk = kFirstChunk;
   int unfetched = 0;
@@ -193,11 +196,19 @@ int row_width(int kind, int n) {
   return Q;
 }
 
+// (vertex, query) pair frontier for graphs of small out-degree whose V * Q
+// pair ids fit 32 bits (as gas_batch chooses it)
+bool use_pairs(const ServeGraph &g, int kind, int Q) {
+  return kind != 2 && g.maxOutDeg <= 64 && (long long)std::max(g.bg.g.nV, 1) * Q < (1ll << 31);
+}
+
 int64_t Server::state_bytes(const ServeGraph &g, int kind, int Q) const {
   const int64_t V = std::max(g.bg.g.nV, 1), W = std::max(Q / 32, 1);
-  // control words, sources, and up to 16 arrays each rounded up to 256 bytes
-  const int64_t base = 256 + 4 * kMaxQ + 16 * 256;
-  const int64_t lists = 24 * gas::detail::batch_list_capacity(V, g.bg.g.nE) + 4 * V;
+  // control words, sources, bucket bounds and flags, and up to 24 arrays
+  // each rounded up to 256 bytes
+  const int64_t base = 256 + 4 * kMaxQ + 4 * (2 * kMaxQ + 24) + 24 * 256;
+  const int64_t lists = 24 * gas::detail::batch_list_capacity(V, g.bg.g.nE) + 4 * V +
+                        (use_pairs(g, kind, Q) ? 12 * V * Q : 0);
   if (kind == 0) return base + V * Q * 4 + 16 * V * W + lists;
   if (kind == 1) return base + V * Q * 4 + 12 * V * W + lists;
   return base + V * Q * 16 + (int64_t)g.pprSlots * Q * 4 + (int64_t)g.pprHubs * 4;
@@ -474,6 +485,12 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     }
     a.inList = reinterpret_cast<int32_t *>(take(Vs * 4));
     a.seen = b.kind == 0 ? reinterpret_cast<unsigned *>(take(Vs * W * 4)) : nullptr;
+    a.pairMode = b.pairs ? 1 : 0;
+    for (int k = 0; k < 3; ++k)
+      a.pairs[k] = b.pairs ? reinterpret_cast<uint32_t *>(take(Vs * b.Q * 4)) : nullptr;
+    a.delta = b.kind == 1 ? b.delta : 0;
+    for (int k = 0; k < 2; ++k) a.thresh[k] = reinterpret_cast<int32_t *>(take(4 * kMaxQ));
+    for (int k = 0; k < 3; ++k) a.nearFlag[k] = reinterpret_cast<unsigned *>(take(4 * 8));
     if (p - b.state > b.stateBytes) return fail(GAS_ERR_STATE, "batch state layout overflow");
     a.cnt = b.ctl->cnt;
     a.barrier = b.ctl->bar;
@@ -484,11 +501,13 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     for (int k = 0; k < 3; ++k) cudaMemsetAsync(a.mask[k], 0, Vs * W * 4, b.stream);
     if (a.seen) cudaMemsetAsync(a.seen, 0, Vs * W * 4, b.stream);
     cudaMemsetAsync(a.inList, 0xff, Vs * 4, b.stream);
+    for (int k = 0; k < 3; ++k) cudaMemsetAsync(a.nearFlag[k], 0, 4 * 8, b.stream);
     const int kb = b.kind == 0 ? gas::detail::kBatchBFS : gas::detail::kBatchSSSP;
-    gas::detail::batch_init_kernel<<<4 * sms, 256, 0, b.stream>>>(kb, V, b.Q, a.value);
+    gas::detail::batch_init_kernel<<<4 * sms, 256, 0, b.stream>>>(kb, V, b.Q, a.value,
+                                                                    a.thresh[0], a.delta);
     gas::detail::batch_sources_kernel<<<(b.nQ + 127) / 128, 128, 0, b.stream>>>(
         kb, b.nQ, b.Q, b.W, b.sources, a.value, a.mask[0], a.seen, g.bg.g.outOff, a.inList,
-        a.list[0], a.listC[0], a.listCnt);
+        a.list[0], a.listC[0], a.listCnt, b.pairs ? a.pairs[0] : nullptr);
   }
   launches += 2;  // init + sources
   e = cudaGetLastError();
@@ -631,6 +650,9 @@ bool Server::admit() {
       bp->nQ = nQ;
       bp->Q = row_width(kind, nQ);
       bp->W = std::max(bp->Q / 32, 1);
+      bp->pairs = use_pairs(*g, kind, bp->Q);
+      // distance buckets for SSSP on pair-frontier (high-diameter) graphs
+      bp->delta = (kind == 1 && bp->pairs) ? 4 * std::max(g->maxWeight, 1) : 0;
       bp->stateBytes = state_bytes(*g, kind, bp->Q);
       bp->outBytes = (int64_t)std::max(g->bg.g.nV, 1) * nQ * 4;
       bp->unfetched = nQ;
@@ -850,6 +872,11 @@ gas_status gas_server_add_graph(gas_server *h, int32_t nVertices, int32_t nEdges
   }
   g->weighted = weights != nullptr;
   g->bytes = need;
+  {
+    const std::vector<int32_t> &off = *g->bg.g.hOutOff;
+    for (int32_t v = 0; v < nVertices; ++v) g->maxOutDeg = std::max(g->maxOutDeg, off[v + 1] - off[v]);
+    for (int32_t i = 0; weights && i < nEdges; ++i) g->maxWeight = std::max(g->maxWeight, weights[i]);
+  }
   std::lock_guard<std::mutex> lk(s.mu);
   g->id = (int32_t)s.graphs.size();
   s.graphs.push_back(g);
