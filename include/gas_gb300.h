@@ -159,6 +159,9 @@ GAS_API gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persisten
  * more than nEdges/alpha out-edges (the reference switches at nEdges/100);
  * 0 keeps every round on frontier lists.  Results do not depend on it. */
 GAS_API gas_status gas_engine_set_dense_policy(gas_engine *e, int32_t alpha);
+/* One-phase list rounds on graphs whose degrees are all <= 8 (default on);
+ * see gas_core_set_fused_rounds.  Results do not depend on it. */
+GAS_API gas_status gas_engine_set_fused_rounds(gas_engine *e, int32_t on);
 
 /* Breadth-first search that allocates nothing (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc -- device memory

@@ -23,6 +23,7 @@
 
 #include "dense.cuh"
 #include "edge_scatter.cuh"
+#include "fused.cuh"
 #include "gather.cuh"
 #include "scatter.cuh"
 
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
   const long long E = a.nEdges;
 
   int cur = ra.cur, sidx = ra.sidx, vcur = 0;
+  bool versioned = false;  // some vertex's newest value sits in the second buffer
   bool rangeMode = a.rangeMode != 0;
   int mode = ra.allActive ? kDense : kList;
   bool allActive = ra.allActive != 0;
@@ -156,6 +158,48 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
       if (n == 0) break;  // uniform: every block read the same count
       bool tpvG;
       const int ntG = gather_tiles(a, n, T, tpvG);
+      if (ra.fused && (tpvG || !a.haveGather)) {
+        // ---------------- fused round: one phase, one barrier
+        FusedCtx f;
+        f.slot[0] = vdBuf[vcur];
+        f.slot[1] = vdBuf[vcur ^ 1];
+        f.ver = ra.ver;
+        f.stamp = (uint32_t)stamp;
+        f.retStamp = ra.retStamp[r & 1];
+        sa.next = ra.frontL[cur ^ 1];
+        sa.stamp = stamp;
+        unsigned cRet = 0u, cOut = 0u;
+        const int ntF = (n + GAS_TPV_TILE - 1) / GAS_TPV_TILE;
+        for (int t = blockIdx.x; t < ntF; t += gridDim.x) {
+          fused_tpv_tile<P>(a, sa, f, t, n, T, sm.s, cRet, cOut);
+          __syncthreads();
+        }
+        cRet = __reduce_add_sync(kFullMask, cRet);
+        cOut = __reduce_add_sync(kFullMask, cOut);
+        unsigned long long *rc = ra.denseCnt + 2 * (r % 3) + 1;
+        if ((threadIdx.x & 31) == 0 && cRet) atomicAdd(rc, ((unsigned long long)cRet << 32) | cOut);
+        versioned = versioned || a.haveGather;
+        if (!grid_barrier(ra.barrier, a.errWord)) break;
+        statA = ((unsigned long long)n << 32) | (unsigned)T;
+        statR = *rc;
+        const int nr = (int)(statR >> 32);
+        denseNext = ra.denseAlpha > 0 && nr > 0 &&
+                    (long long)(statR & 0xffffffffull) * ra.denseAlpha > E;
+        if (denseNext && versioned) {  // dense rounds read the first buffer whole
+          fused_fold<P>(f, a.nVertices);
+          versioned = false;
+          if (!grid_barrier(ra.barrier, a.errWord)) break;
+        }
+      } else {
+      if (versioned) {  // two-phase rounds read the first buffer
+        FusedCtx f;
+        f.slot[0] = vdBuf[vcur];
+        f.slot[1] = vdBuf[vcur ^ 1];
+        f.ver = ra.ver;
+        fused_fold<P>(f, a.nVertices);
+        versioned = false;
+        if (!grid_barrier(ra.barrier, a.errWord)) break;
+      }
       for (int t = blockIdx.x; t < ntG; t += gridDim.x) {
         gather_dispatch<P>(a, t, n, T, tpvG, sm.g);
         __syncthreads();
@@ -199,6 +243,7 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
         }
       }
       if (!grid_barrier(ra.barrier, a.errWord)) break;
+      }  // two-phase round
     } else {
       // ---------------- pull round over every vertex
       dc.vdCur = vdBuf[vcur];
@@ -254,6 +299,13 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
     rangeMode = false;
     cur ^= 1;
     sidx ^= 1;
+  }
+  if (versioned) {  // the newest values into the run's current buffer
+    FusedCtx f;
+    f.slot[0] = vdBuf[vcur];
+    f.slot[1] = vdBuf[vcur ^ 1];
+    f.ver = ra.ver;
+    fused_fold<P>(f, a.nVertices);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *ra.roundsOut = r;

@@ -157,10 +157,12 @@ class EngineGPU {
   // phase and round.
   void setPersistent(bool on) { persistent_ = on; }
 
-  // CTAs per SM of the persistent run kernel (0 = as many as fit).
+  // CTAs per SM of the persistent run kernel (0 = as many as fit; 2 on
+  // graphs whose degrees are all <= 8).
   void setRunBlocksPerSM(int n) {
     runBlocksPerSM_ = n > 0 ? n : 0;
     runGrid_ = 0;
+    runGridFused_ = 0;
   }
 
   // Round number handed to apply(v, g, round) by the stepwise API.
@@ -196,22 +198,29 @@ class EngineGPU {
     return cudaGetLastError() == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
   }
 
+  // Fused-round graphs (small degrees, latency-bound rounds) default to 2
+  // CTAs per SM: a cheaper grid barrier outweighs the lost occupancy.
+  static constexpr int kFusedBlocksPerSM = 2;
+
   static gas_status launchRun(void *user, const gas_run_args *ra, void *stream) {
     EngineGPU *self = static_cast<EngineGPU *>(user);
-    if (self->runGrid_ == 0) {
+    int &grid = ra->fused ? self->runGridFused_ : self->runGrid_;
+    if (grid == 0) {
       int dev = 0, sms = 0, per = 0, coop = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(
           &per, detail::run_persistent_kernel<Program>, detail::kGNT, 0);
-      if (self->runBlocksPerSM_ > 0 && self->runBlocksPerSM_ < per) per = self->runBlocksPerSM_;
-      self->runGrid_ = (coop && per > 0 && sms > 0) ? per * sms : -1;
+      const int want = self->runBlocksPerSM_ > 0 ? self->runBlocksPerSM_
+                                                 : (ra->fused ? kFusedBlocksPerSM : 0);
+      if (want > 0 && want < per) per = want;
+      grid = (coop && per > 0 && sms > 0) ? per * sms : -1;
     }
-    if (self->runGrid_ < 0) return GAS_ERR_UNSUPPORTED;
+    if (grid < 0) return GAS_ERR_UNSUPPORTED;
     void *args[] = {const_cast<gas_run_args *>(ra)};
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)detail::run_persistent_kernel<Program>,
-                                                dim3(self->runGrid_), dim3(detail::kGNT), args,
+                                                dim3(grid), dim3(detail::kGNT), args,
                                                 0, (cudaStream_t)stream);
     if (e == cudaErrorCooperativeLaunchTooLarge) {
       cudaGetLastError();
@@ -238,6 +247,7 @@ class EngineGPU {
   int scatterGrid_ = 0;
   bool persistent_ = true;
   int runGrid_ = 0;
+  int runGridFused_ = 0;
   int runBlocksPerSM_ = 0;
   VertexData *vdHost_ = nullptr;
   EdgeData *edHost_ = nullptr;

@@ -145,6 +145,10 @@ typedef struct {
    * (gas_core_enable_edge_scatter); dense rounds are off then */
   int32_t edgeScatter;
   const int32_t *csr2csc;     /* [E] CSC position of the edge at each CSR position */
+  /* fused list rounds (every degree <= 8): gather, apply and activation in
+   * one phase, vertex data versioned across the two buffers */
+  int32_t fused;
+  uint32_t *ver;              /* [V] (stamp << 1) | buffer of the newest value */
 } gas_run_args;
 
 /* The vertices whose apply returned true in the round just scattered, for
@@ -229,6 +233,11 @@ GAS_API gas_status gas_core_set_profiling(gas_core *c, int32_t enabled);
  * round's apply-returned-true vertices have more than nEdges/alpha
  * out-edges; 0 disables dense rounds.  Results do not depend on it. */
 GAS_API gas_status gas_core_set_dense_policy(gas_core *c, int32_t alpha);
+/* run(): on graphs whose in- and out-degrees are all <= 8, list rounds run
+ * as one phase (gather, apply and activation together, one grid barrier)
+ * with versioned vertex data; 0 keeps the two-phase rounds.  Default on.
+ * Results, round counts and per-round counts do not depend on it. */
+GAS_API gas_status gas_core_set_fused_rounds(gas_core *c, int32_t on);
 GAS_API gas_status gas_core_kernel_times(gas_core *c, float *gatherMs, float *scatterMs,
                                          int32_t *gatherLaunches, int32_t *scatterLaunches);
 /* Waits for queued work and reports device-side errors. */

@@ -361,3 +361,41 @@ def test_bounded_waits_report_timeouts_and_device_recovers(gpu, port):
     g = graphs.rmat(8, 8, seed=9, symmetrize=True)
     depth, _, _ = gpu_bfs(g.n_vertices, g.srcs, g.dsts, 0)
     assert np.array_equal(depth, port.bfs(g.n_vertices, g.srcs, g.dsts, 0)[0])
+
+
+@pytest.mark.parametrize("program", [PROGRAM_SSSP, PROGRAM_BFS, PROGRAM_CC, PROGRAM_PAGERANK])
+def test_fused_rounds_match_two_phase_rounds(gpu, port, program):
+    """One-phase rounds with versioned vertex data (every degree <= 8) give
+    the two-phase rounds' results and per-round counts exactly."""
+    g = graphs.grid(70, 60, 0.15, seed=91, weights=(1, 100))
+    nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
+    out = []
+    for fused in (True, False):
+        if program == PROGRAM_SSSP:
+            vd, act, ed, iters = P.sssp_init(nv, 0), (0, nv), w, 0
+        elif program == PROGRAM_BFS:
+            vd, act, ed, iters = P.bfs_init(nv), (5, 6), None, 0
+        elif program == PROGRAM_CC:
+            vd, act, ed, iters = P.cc_init(nv), (0, nv), None, 0
+        else:
+            vd, act, ed, iters = P.pagerank_init(nv, s), (0, nv), None, 50
+        with GASEngine(program) as e:
+            e.set_graph(nv, vd, s, d, ed)
+            e.set_fused_rounds(fused)
+            e.set_active(*act)
+            rounds = e.run(iters)
+            stats = e.round_stats()
+            e.get_results()
+        out.append((vd.copy(), rounds, stats))
+    (a, ra, sa), (b, rb, sb) = out
+    assert ra == rb
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k]), k
+    if program == PROGRAM_PAGERANK:
+        assert np.array_equal(a["rank"], b["rank"])
+    else:
+        assert np.array_equal(a, b)
+    if program == PROGRAM_SSSP:
+        assert np.array_equal(a, port.sssp(nv, s, d, w, 0)[0])
+    if program == PROGRAM_BFS:
+        assert np.array_equal(a, port.bfs(nv, s, d, 5)[0])

@@ -84,6 +84,7 @@ SIGNATURES = {
     "gas_engine_set_profiling": (_I32, [_P, _I32]),
     "gas_engine_set_launch_config": (_I32, [_P, _I32, _I32]),
     "gas_engine_set_dense_policy": (_I32, [_P, _I32]),
+    "gas_engine_set_fused_rounds": (_I32, [_P, _I32]),
     "gas_engine_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
     "gas_bfs_noalloc": (_I32, [_I32, _I32, _P, _P, _I32, _P, _P, _PI32]),
     "gas_batch_create": (_I32, [_I32, _P, C.POINTER(_P)]),
@@ -144,6 +145,7 @@ SIGNATURES = {
     "gas_core_restore_vertex_data": (_I32, [_P]),
     "gas_core_set_profiling": (_I32, [_P, _I32]),
     "gas_core_set_dense_policy": (_I32, [_P, _I32]),
+    "gas_core_set_fused_rounds": (_I32, [_P, _I32]),
     "gas_core_kernel_times": (_I32, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), _PI32, _PI32]),
     "gas_core_enable_edge_scatter": (_I32, [_P, _I32]),
     "gas_core_edge_scatter": (_I32, [_P, _P, _P]),

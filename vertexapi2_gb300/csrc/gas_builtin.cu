@@ -212,6 +212,11 @@ gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
   return GAS_OK;
 }
 
+gas_status gas_engine_set_fused_rounds(gas_engine *e, int32_t on) {
+  if (!e) return fail(GAS_ERR_INVALID, "engine is NULL");
+  return gas_core_set_fused_rounds(e->impl->core(), on);
+}
+
 gas_status gas_engine_set_dense_policy(gas_engine *e, int32_t alpha) {
   GAS_ENGINE_CHECK(e);
   return gas_core_set_dense_policy(e->impl->core(), alpha);

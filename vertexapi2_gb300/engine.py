@@ -133,6 +133,9 @@ class GASEngine:
     def set_dense_policy(self, alpha: int) -> None:
         check(self._lib.gas_engine_set_dense_policy(self._h, alpha), "gas_engine_set_dense_policy")
 
+    def set_fused_rounds(self, on: bool) -> None:
+        check(self._lib.gas_engine_set_fused_rounds(self._h, int(on)), "gas_engine_set_fused_rounds")
+
     def set_profiling(self, enabled: bool) -> None:
         check(self._lib.gas_engine_set_profiling(self._h, int(enabled)), "gas_engine_set_profiling")
 
