@@ -68,6 +68,11 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
     const VD own1 = load_cg(reinterpret_cast<const VD *>(f.slot[1]) + v);
     const int own = (int)(wv & 1u);  // v is applied once per round: its word is still old
     VD tmp = own ? own1 : own0;
+    // out-neighbours loaded before apply decides whether they are activated
+    const int odeg = oend - obeg;
+    int32_t outd[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) outd[k] = k < odeg ? __ldg(sa.outDests + obeg + k) : 0;
     bool r;
     if (a.haveGather) {
       int src[D];
@@ -96,8 +101,8 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
       cOut += (unsigned)(oend - obeg);
 #pragma unroll
       for (int k = 0; k < D; ++k) {
-        isEdge[k] = k < oend - obeg;
-        dst[k] = isEdge[k] ? __ldg(sa.outDests + obeg + k) : 0;
+        isEdge[k] = k < odeg;
+        dst[k] = outd[k];
       }
     }
   }
