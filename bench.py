@@ -58,6 +58,16 @@ WORKLOADS = {
 SEED = 1
 RMAT_SCALE = {"pagerank-rmat22": 22, "cc-rmat22": 22}
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# run_persistent_kernel from ncu captures of the same command (profiles/):
+# the lattice run directly; PageRank scaled from R-MAT-20 (2.687 GB per
+# launch, 16.09 M edges) by edges, its traffic being per-edge gathers and
+# the CSC stream.  None where no capture exists.
+TRAFFIC_PER_LAUNCH = {
+    "sssp-grid1024": 85.070080e6 + 10.899200e6,
+    "pagerank-rmat22": 2.687299e9 * (65244320 / 16086703),
+}
+
 
 def make_workload(name: str):
     from vertexapi2_gb300 import graphs
@@ -537,7 +547,9 @@ def run_ours(args):
                    "set_graph_ms": set_graph_ms},
         "roofline": {"bound": "hbm", "kernel": "run_persistent_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind,
+                     "traffic": (TRAFFIC_PER_LAUNCH.get(args.workload)
+                                 if RMAT_SCALE.get(args.workload, 22) == 22 else None),
                      "kernel_ms_per_launch": kernel_ms,
                      "algorithmic_bytes_per_launch": run_bytes,
                      "phase_profile_per_launch_kernels": {
