@@ -52,7 +52,8 @@ struct DenseCtx {
   int32_t allActive;       // every vertex active (setActive(0, V))
   int32_t haveGather;
   int32_t iteration;
-  unsigned long long *cnt;  // [2]: (active << 32 | in-edges), (ret << 32 | out-edges)
+  unsigned long long *cnt;  // [3]: (active << 32 | in-edges), (ret << 32 | out-edges),
+                            // work units taken (zero at the start of the pass)
   // degree bins, fixed per graph
   const int32_t *binMid;
   const int32_t *binSmall;
@@ -70,6 +71,11 @@ struct DenseCtx {
 };
 
 constexpr int kChunkEdges = 1024;  // edges per chunk of a large vertex
+constexpr int kDenseCntStride = 4;  // counters per round (DenseCtx::cnt)
+#ifndef GAS_DENSE_GRAB
+#define GAS_DENSE_GRAB 4
+#endif
+constexpr int kDenseGrab = GAS_DENSE_GRAB;  // work units a warp takes at a time (0: static)
 constexpr int kSmallLanes = 8;     // lanes per vertex of in-degree 9..64
 
 // Per-lane accumulators of one edge stream: reduction, "has an edge",
@@ -309,14 +315,28 @@ __device__ __forceinline__ void dense_flush(const DenseCtx &a, const DenseCounts
   }
 }
 
-// One dense pass over every vertex, warp units assigned statically.
+// One dense pass over every vertex.  Warps take kDenseGrab work units at a
+// time from a counter, heaviest first (chunks, then the bins in descending
+// in-degree), so the pass ends on small units.
 template <class P>
 __device__ void dense_pass(const DenseCtx &a) {
   DenseCounts c = {0u, 0u, 0u, 0u};
-  const long long units = dense_units(a);
-  const long long warps = (long long)gridDim.x * (blockDim.x / 32);
-  for (long long u = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; u < units; u += warps)
-    dense_warp_unit<P>(a, u, c);
+  const unsigned long long units = (unsigned long long)dense_units(a);
+  if constexpr (kDenseGrab == 0) {  // static round-robin assignment
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    for (unsigned long long u = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; u < units; u += warps)
+      dense_warp_unit<P>(a, (long long)u, c);
+    dense_flush(a, c);
+    return;
+  }
+  for (;;) {
+    unsigned long long u0 = 0ull;
+    if ((threadIdx.x & 31) == 0) u0 = atomicAdd(a.cnt + 2, (unsigned long long)kDenseGrab);
+    u0 = __shfl_sync(kFullMask, u0, 0);
+    if (u0 >= units) break;
+    const unsigned long long u1 = min(u0 + kDenseGrab, units);
+    for (unsigned long long u = u0; u < u1; ++u) dense_warp_unit<P>(a, (long long)u, c);
+  }
   dense_flush(a, c);
 }
 

@@ -138,9 +138,10 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
       *ra.scatL[sidx ^ 1].count = 0ull;  // appended by the next round's gather
       *ra.scatL[sidx ^ 1].maxDeg = 0u;
       if (ra.denseCnt) {  // absent when dense rounds are disabled
-        unsigned long long *nextCnt = ra.denseCnt + 2 * ((r + 1) % 3);
+        unsigned long long *nextCnt = ra.denseCnt + kDenseCntStride * ((r + 1) % 3);
         nextCnt[0] = 0ull;
         nextCnt[1] = 0ull;
+        nextCnt[2] = 0ull;
       }
     }
     unsigned long long statA, statR;
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
         }
         cRet = __reduce_add_sync(kFullMask, cRet);
         cOut = __reduce_add_sync(kFullMask, cOut);
-        unsigned long long *rc = ra.denseCnt + 2 * (r % 3) + 1;
+        unsigned long long *rc = ra.denseCnt + kDenseCntStride * (r % 3) + 1;
         if ((threadIdx.x & 31) == 0 && cRet) atomicAdd(rc, ((unsigned long long)cRet << 32) | cOut);
         versioned = versioned || a.haveGather;
         if (!grid_barrier(ra.barrier, a.errWord)) break;
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_a
       dc.curStamp = stamp;
       dc.allActive = allActive ? 1 : 0;
       dc.iteration = ra.g.iteration + r;
-      dc.cnt = ra.denseCnt + 2 * (r % 3);
+      dc.cnt = ra.denseCnt + kDenseCntStride * (r % 3);
       dense_pass<P>(dc);
       if (!grid_barrier(ra.barrier, a.errWord)) break;
       statA = dc.cnt[0];

@@ -121,7 +121,8 @@ typedef struct {
   void *vertexAlt;            /* second vertex-data buffer (ping-pong)      */
   int32_t *retStamp[2];       /* [V] each: stamp of the round whose apply returned
                                  true; round r writes [r & 1] and reads [(r-1) & 1] */
-  unsigned long long *denseCnt; /* [3][2] per-round counters                */
+  unsigned long long *denseCnt; /* [3][4] per-round counters: active/in-edges,
+                                 ret/out-edges, dense work units taken, unused */
   int32_t denseAlpha;         /* next round dense when out-edges*alpha > E; 0 = never */
   int32_t allActive;          /* round 0 is every vertex (setActive(0, V)) */
   int32_t *vcurOut;           /* 1 when the final vertex data is in vertexAlt */

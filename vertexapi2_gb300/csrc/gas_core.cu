@@ -93,7 +93,7 @@ struct Ctl {
   unsigned bar[2];  // persistent-kernel grid barrier: arrivals, generation
   int32_t rounds;   // rounds executed by the last persistent run
   int32_t vcur;     // 1 when that run's result is in the alternate buffer
-  unsigned long long dense[3][2];  // per-round counters of dense rounds
+  unsigned long long dense[3][4];  // per-round counters of dense rounds (kDenseCntStride)
   unsigned err;     // device error bits (kept across set_active)
   unsigned pad;
 };
@@ -528,6 +528,12 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
       }
     }
   }
+  // heaviest first: the dense pass hands out work units in this order
+  const auto byInDegDesc = [c](int32_t x, int32_t y) {
+    return c->hInOff[(size_t)x + 1] - c->hInOff[x] > c->hInOff[(size_t)y + 1] - c->hInOff[y];
+  };
+  std::stable_sort(bMid.begin(), bMid.end(), byInDegDesc);
+  std::stable_sort(bSmall.begin(), bSmall.end(), byInDegDesc);
   c->nMid = (int32_t)bMid.size();
   c->nSmall = (int32_t)bSmall.size();
   c->nTiny = (int32_t)bTiny.size();
