@@ -148,8 +148,9 @@ GAS_API gas_status gas_engine_kernel_times(gas_engine *e, float *gatherMs, float
 
 /* Launch shape of run(): persistent != 0 runs every round in one
  * cooperative kernel (the default), 0 launches each phase of each round;
- * runBlocksPerSM bounds the persistent kernel's CTAs per SM (0 = as many as
- * fit).  Results do not depend on either. */
+ * runBlocksPerSM bounds the persistent kernel's CTAs per SM (0 = the
+ * default: 2 on graphs whose degrees are all <= 8, else 4).  Results do not
+ * depend on either. */
 GAS_API gas_status gas_engine_set_launch_config(gas_engine *e, int32_t persistent,
                                                 int32_t runBlocksPerSM);
 

@@ -72,10 +72,7 @@ struct DenseCtx {
 
 constexpr int kChunkEdges = 1024;  // edges per chunk of a large vertex
 constexpr int kDenseCntStride = 4;  // counters per round (DenseCtx::cnt)
-#ifndef GAS_DENSE_GRAB
-#define GAS_DENSE_GRAB 4
-#endif
-constexpr int kDenseGrab = GAS_DENSE_GRAB;  // work units a warp takes at a time (0: static)
+constexpr int kDenseGrab = 4;  // work units a warp takes at a time
 constexpr int kSmallLanes = 8;     // lanes per vertex of in-degree 9..64
 
 // Per-lane accumulators of one edge stream: reduction, "has an edge",
@@ -121,29 +118,39 @@ __device__ __forceinline__ void group_reduce(EdgeAcc<typename P::GatherResult> &
   }
 }
 
-// Lane-strided walk of the edges [beg, end) of vertex v, four edges per
-// lane in flight: all source ids first, then their stamps and data.
+// Lane-strided walk of the edges [beg, end) of vertex v by a whole warp,
+// kStrideDepth edges per lane in flight: all source ids first, then their
+// stamps and data.  Once some lane has seen an activating in-neighbour the
+// vertex is known active and the remaining stamps are not read.
+constexpr int kStrideDepth = 4;
+
 template <class P>
 __device__ __forceinline__ void strided_edges(const DenseCtx &a, int v, int beg, int end,
                                               EdgeAcc<typename P::GatherResult> &x) {
+  typedef typename P::VertexData VD;
+  constexpr int J = kStrideDepth;
   const int lane = threadIdx.x & 31;
-  for (int e0 = beg + lane; e0 < end; e0 += 4 * 32) {
-    int src[4];
+  const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
+  bool known = a.allActive != 0;  // warp-uniform
+  for (int base = beg; base < end; base += J * 32) {
+    int src[J];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) src[j] = (e0 + 32 * j < end) ? __ldg(a.inSources + e0 + 32 * j) : -1;
+    for (int j = 0; j < J; ++j) {
+      const int e = base + lane + 32 * j;
+      src[j] = e < end ? __ldg(a.inSources + e) : -1;
+    }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < J; ++j) {
       if (src[j] < 0) continue;
-      typedef typename P::VertexData VD;
-      const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
-      x.act |= (a.allActive || a.prevRet[src[j]] == a.prevStamp) ? 1u : 0u;
+      x.act |= (known || a.prevRet[src[j]] == a.prevStamp) ? 1u : 0u;
       if (a.haveGather) {
         const typename P::GatherResult m =
-            P::gatherMap(vd + v, vd + src[j], edge_ptr<P>(a.edgeData, e0 + 32 * j));
+            P::gatherMap(vd + v, vd + src[j], edge_ptr<P>(a.edgeData, base + lane + 32 * j));
         x.val = x.has ? P::gatherReduce(x.val, m) : m;
       }
       x.has = 1u;
     }
+    known = __any_sync(kFullMask, x.act != 0u);
   }
 }
 
@@ -315,27 +322,31 @@ __device__ __forceinline__ void dense_flush(const DenseCtx &a, const DenseCounts
   }
 }
 
-// One dense pass over every vertex.  Warps take kDenseGrab work units at a
-// time from a counter, heaviest first (chunks, then the bins in descending
-// in-degree), so the pass ends on small units.
+// One dense pass over every vertex, heaviest work units first (chunks, then
+// the bins in descending in-degree).  The first kDenseGrab units of every
+// warp are dealt round-robin; past them warps take kDenseGrab consecutive
+// units at a time from a counter, so the pass ends on small units.
 template <class P>
 __device__ void dense_pass(const DenseCtx &a) {
   DenseCounts c = {0u, 0u, 0u, 0u};
   const unsigned long long units = (unsigned long long)dense_units(a);
-  if constexpr (kDenseGrab == 0) {  // static round-robin assignment
-    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
-    for (unsigned long long u = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; u < units; u += warps)
-      dense_warp_unit<P>(a, (long long)u, c);
-    dense_flush(a, c);
-    return;
+  const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+  const unsigned long long w = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+#pragma unroll 1
+  for (int k = 0; k < kDenseGrab; ++k) {
+    const unsigned long long u = w + k * warps;
+    if (u >= units) break;
+    dense_warp_unit<P>(a, (long long)u, c);
   }
-  for (;;) {
-    unsigned long long u0 = 0ull;
-    if ((threadIdx.x & 31) == 0) u0 = atomicAdd(a.cnt + 2, (unsigned long long)kDenseGrab);
-    u0 = __shfl_sync(kFullMask, u0, 0);
-    if (u0 >= units) break;
-    const unsigned long long u1 = min(u0 + kDenseGrab, units);
-    for (unsigned long long u = u0; u < u1; ++u) dense_warp_unit<P>(a, (long long)u, c);
+  if (warps * kDenseGrab < units) {
+    for (;;) {
+      unsigned long long u0 = 0ull;
+      if ((threadIdx.x & 31) == 0) u0 = warps * kDenseGrab + atomicAdd(a.cnt + 2, (unsigned long long)kDenseGrab);
+      u0 = __shfl_sync(kFullMask, u0, 0);
+      if (u0 >= units) break;
+      const unsigned long long u1 = min(u0 + kDenseGrab, units);
+      for (unsigned long long u = u0; u < u1; ++u) dense_warp_unit<P>(a, (long long)u, c);
+    }
   }
   dense_flush(a, c);
 }

@@ -73,9 +73,10 @@ union PersistentSmem {
   ScatterSmem s;
 };
 
-// 3 CTAs of 256 threads per SM (<= 85 registers a thread).
-template <class P>
-__global__ void __launch_bounds__(kGNT, 3) run_persistent_kernel(const gas_run_args ra) {
+// MinBlocks CTAs of 256 threads per SM: the register budget a thread gets
+// (2: 128, 3: 80, 4: 64).
+template <class P, int MinBlocks = 3>
+__global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const gas_run_args ra) {
   enum { kList = 0, kDense = 1 };
   __shared__ PersistentSmem<P> sm;
   gas_gather_args a = ra.g;

@@ -157,8 +157,8 @@ class EngineGPU {
   // phase and round.
   void setPersistent(bool on) { persistent_ = on; }
 
-  // CTAs per SM of the persistent run kernel (0 = as many as fit; 2 on
-  // graphs whose degrees are all <= 8).
+  // CTAs per SM of the persistent run kernel (0 = the default: 2 on graphs
+  // whose degrees are all <= 8, else 4; at most what fits).
   void setRunBlocksPerSM(int n) {
     runBlocksPerSM_ = n > 0 ? n : 0;
     runGrid_ = 0;
@@ -198,29 +198,33 @@ class EngineGPU {
     return cudaGetLastError() == cudaSuccess ? GAS_OK : GAS_ERR_CUDA;
   }
 
-  // Fused-round graphs (small degrees, latency-bound rounds) default to 2
-  // CTAs per SM: a cheaper grid barrier outweighs the lost occupancy.
+  // CTAs per SM of the persistent kernel.  Fused-round graphs (small
+  // degrees, latency-bound rounds) run 2 with 128 registers a thread: a
+  // cheaper grid barrier outweighs the lost occupancy.  Other graphs run 4
+  // with 64 registers: more warps in flight for the pull passes, whose
+  // dependent gathers are L2-latency bound.
   static constexpr int kFusedBlocksPerSM = 2;
+  static constexpr int kRunBlocksPerSM = 4;
 
   static gas_status launchRun(void *user, const gas_run_args *ra, void *stream) {
     EngineGPU *self = static_cast<EngineGPU *>(user);
     int &grid = ra->fused ? self->runGridFused_ : self->runGrid_;
+    const void *kern = ra->fused ? (const void *)detail::run_persistent_kernel<Program, kFusedBlocksPerSM>
+                                 : (const void *)detail::run_persistent_kernel<Program, kRunBlocksPerSM>;
     if (grid == 0) {
       int dev = 0, sms = 0, per = 0, coop = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per, detail::run_persistent_kernel<Program>, detail::kGNT, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, detail::kGNT, 0);
       const int want = self->runBlocksPerSM_ > 0 ? self->runBlocksPerSM_
-                                                 : (ra->fused ? kFusedBlocksPerSM : 0);
+                                                 : (ra->fused ? kFusedBlocksPerSM : kRunBlocksPerSM);
       if (want > 0 && want < per) per = want;
       grid = (coop && per > 0 && sms > 0) ? per * sms : -1;
     }
     if (grid < 0) return GAS_ERR_UNSUPPORTED;
     void *args[] = {const_cast<gas_run_args *>(ra)};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)detail::run_persistent_kernel<Program>,
-                                                dim3(grid), dim3(detail::kGNT), args,
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(detail::kGNT), args,
                                                 0, (cudaStream_t)stream);
     if (e == cudaErrorCooperativeLaunchTooLarge) {
       cudaGetLastError();

@@ -1,80 +1,13 @@
 // Engine layer of the C ABI (gas_gb300.h): gas_engine_* for the built-in
 // vertex programs.  Each program id maps to gas::EngineGPU<Program> (the
 // same template a C++ user instantiates from gas_gb300/gpugas.cuh), so the
-// FFI path and the C++ path run identical kernels.
-#include <new>
-
-#include "gas_gb300.h"
-#include "gas_gb300/gpugas.cuh"
-#include "gas_gb300/programs.cuh"
+// FFI path and the C++ path run identical kernels; the engines are made in
+// gas_program_*.cu.
+#include "gas_builtin_engine.h"
 #include "gas_internal.h"
 
+using gas::internal::EngineBase;
 using gas::internal::fail;
-
-namespace {
-
-struct EngineBase {
-  virtual ~EngineBase() {}
-  virtual gas_status status() const = 0;
-  virtual gas_core *core() = 0;
-  virtual gas_status setGraph(int32_t nV, void *vd, int32_t nE, void *ed, const int32_t *s,
-                              const int32_t *d) = 0;
-  virtual gas_status getResults() = 0;
-  virtual gas_status setActive(int32_t a, int32_t b) = 0;
-  virtual gas_status countActive(int32_t *n) = 0;
-  virtual gas_status gatherApply(bool g) = 0;
-  virtual gas_status scatterActivate(bool s) = 0;
-  virtual gas_status nextIter(int32_t *n) = 0;
-  virtual gas_status run(int32_t maxIters, int32_t *iters) = 0;
-  virtual void setLaunch(bool persistent, int blocksPerSM) = 0;
-};
-
-template <class P>
-struct BuiltinEngine final : EngineBase {
-  gas::EngineGPU<P> eng;
-  BuiltinEngine(int device, cudaStream_t stream) : eng(device, stream) {}
-  gas_status status() const override { return eng.lastStatus(); }
-  gas_core *core() override { return eng.core(); }
-  gas_status setGraph(int32_t nV, void *vd, int32_t nE, void *ed, const int32_t *s,
-                      const int32_t *d) override {
-    eng.setGraph(nV, reinterpret_cast<typename P::VertexData *>(vd), nE,
-                 reinterpret_cast<typename P::EdgeData *>(ed), s, d);
-    return eng.lastStatus();
-  }
-  gas_status getResults() override {
-    eng.getResults();
-    return eng.lastStatus();
-  }
-  gas_status setActive(int32_t a, int32_t b) override {
-    eng.setActive(a, b);
-    return eng.lastStatus();
-  }
-  gas_status countActive(int32_t *n) override { return gas_core_count_active(eng.core(), n); }
-  gas_status gatherApply(bool g) override {
-    eng.gatherApply(g);
-    return eng.lastStatus();
-  }
-  gas_status scatterActivate(bool s) override {
-    eng.scatterActivate(s);
-    return eng.lastStatus();
-  }
-  gas_status nextIter(int32_t *n) override {
-    gas_status st = gas_core_next_iter(eng.core());
-    if (st || !n) return st;
-    return gas_core_count_active(eng.core(), n);
-  }
-  gas_status run(int32_t maxIters, int32_t *iters) override {
-    int32_t it = eng.runFor(maxIters);
-    if (iters) *iters = it;
-    return eng.lastStatus();
-  }
-  void setLaunch(bool persistent, int blocksPerSM) override {
-    eng.setPersistent(persistent);
-    eng.setRunBlocksPerSM(blocksPerSM);
-  }
-};
-
-}  // namespace
 
 struct gas_engine_s {
   int32_t program;
@@ -89,11 +22,11 @@ gas_status gas_engine_create(int32_t program, int32_t device, void *stream, gas_
   EngineBase *impl = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
   switch (program) {
-    case GAS_PROGRAM_BFS: impl = new (std::nothrow) BuiltinEngine<gas::programs::BFS>(device, s); break;
-    case GAS_PROGRAM_SSSP: impl = new (std::nothrow) BuiltinEngine<gas::programs::SSSP>(device, s); break;
-    case GAS_PROGRAM_CC: impl = new (std::nothrow) BuiltinEngine<gas::programs::CC>(device, s); break;
-    case GAS_PROGRAM_PAGERANK: impl = new (std::nothrow) BuiltinEngine<gas::programs::PageRank>(device, s); break;
-    case GAS_PROGRAM_PPR: impl = new (std::nothrow) BuiltinEngine<gas::programs::PPR>(device, s); break;
+    case GAS_PROGRAM_BFS: impl = gas::internal::new_engine_bfs(device, s); break;
+    case GAS_PROGRAM_SSSP: impl = gas::internal::new_engine_sssp(device, s); break;
+    case GAS_PROGRAM_CC: impl = gas::internal::new_engine_cc(device, s); break;
+    case GAS_PROGRAM_PAGERANK: impl = gas::internal::new_engine_pagerank(device, s); break;
+    case GAS_PROGRAM_PPR: impl = gas::internal::new_engine_ppr(device, s); break;
     default: return fail(GAS_ERR_INVALID, "unknown program id %d", program);
   }
   if (!impl) return fail(GAS_ERR_OOM, "host allocation");
@@ -146,7 +79,7 @@ gas_status gas_engine_set_active(gas_engine *e, int32_t vertexStart, int32_t ver
 gas_status gas_engine_count_active(gas_engine *e, int32_t *nActive) {
   GAS_ENGINE_CHECK(e);
   if (!nActive) return fail(GAS_ERR_INVALID, "nActive is NULL");
-  return e->impl->countActive(nActive);
+  return gas_core_count_active(e->impl->core(), nActive);
 }
 
 gas_status gas_engine_gather_apply(gas_engine *e, int32_t haveGather) {
@@ -161,7 +94,9 @@ gas_status gas_engine_scatter_activate(gas_engine *e, int32_t haveScatter) {
 
 gas_status gas_engine_next_iter(gas_engine *e, int32_t *nActive) {
   GAS_ENGINE_CHECK(e);
-  return e->impl->nextIter(nActive);
+  gas_status st = gas_core_next_iter(e->impl->core());
+  if (st || !nActive) return st;
+  return gas_core_count_active(e->impl->core(), nActive);
 }
 
 gas_status gas_engine_run(gas_engine *e, int32_t maxIters, int32_t *iterations) {
