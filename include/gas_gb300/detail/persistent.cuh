@@ -73,6 +73,145 @@ union PersistentSmem {
   ScatterSmem s;
 };
 
+// The fixed part of a dense pass's context (graph, degree bins, chunks).
+__device__ __forceinline__ DenseCtx dense_ctx(const gas_run_args &ra) {
+  DenseCtx dc;
+  dc.nVertices = ra.g.nVertices;
+  dc.nEdges = ra.g.nEdges;
+  dc.inOffsets = ra.g.inOffsets;
+  dc.inSources = ra.g.inSources;
+  dc.outOffsets = ra.g.outOffsets;
+  dc.edgeData = ra.g.edgeData;
+  dc.binMid = ra.binMid;
+  dc.binSmall = ra.binSmall;
+  dc.binTiny = ra.binTiny;
+  dc.nMid = ra.nMid;
+  dc.nSmall = ra.nSmall;
+  dc.nTiny = ra.nTiny;
+  dc.chunkVertex = ra.chunkVertex;
+  dc.chunkBegin = ra.chunkBegin;
+  dc.chunkFirst = ra.chunkFirst;
+  dc.chunkCount = ra.chunkCount;
+  dc.chunkSlot = ra.chunkSlot;
+  dc.nChunks = ra.nChunks;
+  dc.chunkArrive = ra.chunkArrive;
+  dc.chunkVal = ra.chunkVal;
+  dc.chunkFlags = ra.chunkFlags;
+  dc.haveGather = ra.g.haveGather;
+  return dc;
+}
+
+// Round r's per-round settings of a dense pass over vdBuf[vcur].
+__device__ __forceinline__ void dense_round(DenseCtx &dc, const gas_run_args &ra, void *const vdBuf[2],
+                                            int vcur, int r, bool allActive) {
+  const int32_t stamp = ra.stampBase + r;
+  dc.vdCur = vdBuf[vcur];
+  dc.vdNext = vdBuf[vcur ^ 1];
+  dc.prevRet = ra.retStamp[(r + 1) & 1];
+  dc.curRet = ra.retStamp[r & 1];
+  dc.prevStamp = stamp - 1;
+  dc.curStamp = stamp;
+  dc.allActive = allActive ? 1 : 0;
+  dc.iteration = ra.g.iteration + r;
+  dc.cnt = ra.denseCnt + kDenseCntStride * (r % 3);
+}
+
+// Round-start resets by one thread: the lists this round appends to and the
+// next round's dense counters.
+__device__ __forceinline__ void round_resets(const gas_run_args &ra, int r, int cur, int sidx) {
+  *ra.frontL[cur ^ 1].count = 0ull;  // appended by this round's scatter
+  *ra.frontL[cur ^ 1].maxDeg = 0u;
+  *ra.scatL[sidx ^ 1].count = 0ull;  // appended by the next round's gather
+  *ra.scatL[sidx ^ 1].maxDeg = 0u;
+  if (ra.denseCnt) {  // absent when dense rounds are disabled
+    unsigned long long *nextCnt = ra.denseCnt + kDenseCntStride * ((r + 1) % 3);
+    nextCnt[0] = 0ull;
+    nextCnt[1] = 0ull;
+    nextCnt[2] = 0ull;
+  }
+}
+
+// Dense -> list transition at the end of dense round r (stamp): the
+// vertices stamped in it become scatL[sidx] (vertex order per block) and
+// are pushed into frontL[cur ^ 1].  False when a grid barrier gave up.
+template <class P>
+__device__ __forceinline__ bool dense_to_list(const gas_run_args &ra, const gas_gather_args &a,
+                                              ScatterArgs &sa, PersistentSmem<P> &sm, int r, int cur,
+                                              int sidx) {
+  const int32_t stamp = ra.stampBase + r;
+  compact_ret<kGNT, kGVT>(ra.retStamp[r & 1], stamp, a.outOffsets, a.nVertices, ra.scatL[sidx],
+                          a.maxScatTiles, a.errWord, sm.g.app);
+  if (!grid_barrier(ra.barrier, a.errWord)) return false;
+  const unsigned long long sc = *ra.scatL[sidx].count;
+  int ns = (int)(sc >> 32);
+  if (ns > a.capacity) ns = a.capacity;
+  const int Ts = (int)(sc & 0xffffffffull);
+  sa.commit = 0;
+  sa.scat = ra.scatL[sidx];
+  sa.next = ra.frontL[cur ^ 1];
+  sa.stamp = stamp;
+  bool tpvS;
+  const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
+  for (int t = blockIdx.x; t < ntS; t += gridDim.x) {
+    if (tpvS)
+      tpv_scatter_tile(sa, t, ns, Ts, sm.s);
+    else
+      scatter_tile(sa, t, ns, Ts, sm.s);
+    __syncthreads();
+  }
+  return grid_barrier(ra.barrier, a.errWord);
+}
+
+// The leading dense rounds of a run that starts with every vertex active,
+// in a kernel that holds nothing else: 40 registers a thread, 6 CTAs per SM
+// (the main kernel's list-round code needs 64 or more).  It stops before
+// the first list round and leaves ra.resume for the main kernel; the
+// rounds, stamps, resets and statistics are the main kernel's own.
+template <class P, int MinBlocks>
+__global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_run_args ra) {
+  DenseCtx dc = dense_ctx(ra);
+  void *const vdBuf[2] = {ra.g.vertexData, ra.vertexAlt};
+  const long long E = ra.g.nEdges;
+  int vcur = 0, r = 0, pending = 0, ended = 0;
+  for (;;) {
+    if (ra.maxRounds > 0 && r >= ra.maxRounds) {
+      ended = 1;
+      break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, ra.cur ^ (r & 1), ra.sidx ^ (r & 1));
+    dense_round(dc, ra, vdBuf, vcur, r, r == 0);
+    dense_pass<P>(dc);
+    if (!grid_barrier(ra.barrier, ra.g.errWord)) {
+      ended = 1;
+      break;
+    }
+    const unsigned long long statA = dc.cnt[0], statR = dc.cnt[1];
+    if ((statA >> 32) == 0) {  // no vertex was active: the run ended before this round
+      ended = 1;
+      break;
+    }
+    vcur ^= 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && r < ra.maxStatRounds) {
+      ra.stats[2 * (size_t)r] = statA;
+      ra.stats[2 * (size_t)r + 1] = statR;
+    }
+    ++r;
+    const int nr = (int)(statR >> 32);
+    const long long eout = (long long)(statR & 0xffffffffull);
+    if (!(ra.denseAlpha > 0 && nr > 0 && eout * ra.denseAlpha > E)) {
+      pending = nr > 0 ? 1 : 0;  // else the next (list) round is empty
+      ended = 1 - pending;
+      break;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ra.resume[0] = r;
+    ra.resume[1] = vcur;
+    ra.resume[2] = pending;
+    ra.resume[3] = ended;
+  }
+}
+
 // MinBlocks CTAs of 256 threads per SM: the register budget a thread gets
 // (2: 128, 3: 80, 4: 64).
 template <class P, int MinBlocks = 3>
@@ -97,29 +236,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   sa.resetScatMaxDeg = nullptr;
   sa.errWord = a.errWord;
   sa.statSlot = nullptr;
-  DenseCtx dc;
-  dc.nVertices = a.nVertices;
-  dc.nEdges = a.nEdges;
-  dc.inOffsets = a.inOffsets;
-  dc.inSources = a.inSources;
-  dc.outOffsets = a.outOffsets;
-  dc.edgeData = a.edgeData;
-  dc.binMid = ra.binMid;
-  dc.binSmall = ra.binSmall;
-  dc.binTiny = ra.binTiny;
-  dc.nMid = ra.nMid;
-  dc.nSmall = ra.nSmall;
-  dc.nTiny = ra.nTiny;
-  dc.chunkVertex = ra.chunkVertex;
-  dc.chunkBegin = ra.chunkBegin;
-  dc.chunkFirst = ra.chunkFirst;
-  dc.chunkCount = ra.chunkCount;
-  dc.chunkSlot = ra.chunkSlot;
-  dc.nChunks = ra.nChunks;
-  dc.chunkArrive = ra.chunkArrive;
-  dc.chunkVal = ra.chunkVal;
-  dc.chunkFlags = ra.chunkFlags;
-  dc.haveGather = a.haveGather;
+  DenseCtx dc = dense_ctx(ra);
   void *vdBuf[2] = {a.vertexData, ra.vertexAlt};
   const long long E = a.nEdges;
 
@@ -129,22 +246,23 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   int mode = ra.allActive ? kDense : kList;
   bool allActive = ra.allActive != 0;
   int r = 0;
+  bool ended = false;
+  if (ra.denseFirst) {  // resume after run_dense_kernel's rounds
+    r = ra.resume[0];
+    vcur = ra.resume[1];
+    ended = ra.resume[3] != 0;
+    cur = ra.cur ^ (r & 1);
+    sidx = ra.sidx ^ (r & 1);
+    mode = kList;
+    allActive = false;
+    rangeMode = false;
+    if (ra.resume[2] && !ended && !dense_to_list<P>(ra, a, sa, sm, r - 1, cur ^ 1, sidx ^ 1)) ended = true;
+  }
   for (;;) {
-    if (ra.maxRounds > 0 && r >= ra.maxRounds) break;
+    if (ended || (ra.maxRounds > 0 && r >= ra.maxRounds)) break;
     const unsigned epoch = ra.epochBase + (unsigned)r;
     const int32_t stamp = ra.stampBase + r;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      *ra.frontL[cur ^ 1].count = 0ull;  // appended by this round's scatter
-      *ra.frontL[cur ^ 1].maxDeg = 0u;
-      *ra.scatL[sidx ^ 1].count = 0ull;  // appended by the next round's gather
-      *ra.scatL[sidx ^ 1].maxDeg = 0u;
-      if (ra.denseCnt) {  // absent when dense rounds are disabled
-        unsigned long long *nextCnt = ra.denseCnt + kDenseCntStride * ((r + 1) % 3);
-        nextCnt[0] = 0ull;
-        nextCnt[1] = 0ull;
-        nextCnt[2] = 0ull;
-      }
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, cur, sidx);
     unsigned long long statA, statR;
     bool denseNext;
     if (mode == kList) {
@@ -248,15 +366,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       }  // two-phase round
     } else {
       // ---------------- pull round over every vertex
-      dc.vdCur = vdBuf[vcur];
-      dc.vdNext = vdBuf[vcur ^ 1];
-      dc.prevRet = ra.retStamp[(r + 1) & 1];
-      dc.curRet = ra.retStamp[r & 1];
-      dc.prevStamp = stamp - 1;
-      dc.curStamp = stamp;
-      dc.allActive = allActive ? 1 : 0;
-      dc.iteration = ra.g.iteration + r;
-      dc.cnt = ra.denseCnt + kDenseCntStride * (r % 3);
+      dense_round(dc, ra, vdBuf, vcur, r, allActive);
       dense_pass<P>(dc);
       if (!grid_barrier(ra.barrier, a.errWord)) break;
       statA = dc.cnt[0];
@@ -268,27 +378,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       denseNext = ra.denseAlpha > 0 && nr > 0 && eout * ra.denseAlpha > E;
       if (!denseNext && nr > 0) {
         // dense -> list: compact the stamped vertices, then push them
-        compact_ret<kGNT, kGVT>(ra.retStamp[r & 1], stamp, a.outOffsets, a.nVertices, ra.scatL[sidx],
-                                a.maxScatTiles, a.errWord, sm.g.app);
-        if (!grid_barrier(ra.barrier, a.errWord)) break;
-        const unsigned long long sc = *ra.scatL[sidx].count;
-        int ns = (int)(sc >> 32);
-        if (ns > a.capacity) ns = a.capacity;
-        const int Ts = (int)(sc & 0xffffffffull);
-        sa.commit = 0;
-        sa.scat = ra.scatL[sidx];
-        sa.next = ra.frontL[cur ^ 1];
-        sa.stamp = stamp;
-        bool tpvS;
-        const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
-        for (int t = blockIdx.x; t < ntS; t += gridDim.x) {
-          if (tpvS)
-            tpv_scatter_tile(sa, t, ns, Ts, sm.s);
-          else
-            scatter_tile(sa, t, ns, Ts, sm.s);
-          __syncthreads();
-        }
-        if (!grid_barrier(ra.barrier, a.errWord)) break;
+        if (!dense_to_list<P>(ra, a, sa, sm, r, cur, sidx)) break;
       }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && r < ra.maxStatRounds) {

@@ -205,9 +205,41 @@ class EngineGPU {
   // dependent gathers are L2-latency bound.
   static constexpr int kFusedBlocksPerSM = 2;
   static constexpr int kRunBlocksPerSM = 4;
+  // A run that starts with every vertex active runs its leading dense rounds
+  // in run_dense_kernel (40 registers, 6 CTAs per SM), then resumes here.
+#ifndef GAS_DENSE_BLOCKS_PER_SM
+#define GAS_DENSE_BLOCKS_PER_SM 6
+#endif
+  static constexpr int kDenseBlocksPerSM = GAS_DENSE_BLOCKS_PER_SM;
 
   static gas_status launchRun(void *user, const gas_run_args *ra, void *stream) {
     EngineGPU *self = static_cast<EngineGPU *>(user);
+    if (ra->allActive && ra->resume && !ra->denseFirst && self->runBlocksPerSM_ == 0) {
+      const void *dk = (const void *)detail::run_dense_kernel<Program, kDenseBlocksPerSM>;
+      if (self->denseGrid_ == 0) {
+        int dev = 0, sms = 0, per = 0, coop = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, dk, detail::kGNT, 0);
+        if (per > kDenseBlocksPerSM) per = kDenseBlocksPerSM;
+        self->denseGrid_ = (coop && per > 0 && sms > 0) ? per * sms : -1;
+      }
+      if (self->denseGrid_ > 0) {
+        void *dargs[] = {const_cast<gas_run_args *>(ra)};
+        cudaError_t e = cudaLaunchCooperativeKernel(dk, dim3(self->denseGrid_), dim3(detail::kGNT), dargs, 0,
+                                                    (cudaStream_t)stream);
+        if (e == cudaSuccess) {
+          gas_run_args rest = *ra;
+          rest.denseFirst = 1;
+          const gas_status st = launchRun(user, &rest, stream);
+          // rounds already ran: a per-phase fallback would repeat them
+          return st == GAS_ERR_UNSUPPORTED ? GAS_ERR_CUDA : st;
+        }
+        cudaGetLastError();
+        self->denseGrid_ = -1;  // not co-resident: the main kernel runs every round
+      }
+    }
     int &grid = ra->fused ? self->runGridFused_ : self->runGrid_;
     const void *kern = ra->fused ? (const void *)detail::run_persistent_kernel<Program, kFusedBlocksPerSM>
                                  : (const void *)detail::run_persistent_kernel<Program, kRunBlocksPerSM>;
@@ -252,6 +284,7 @@ class EngineGPU {
   bool persistent_ = true;
   int runGrid_ = 0;
   int runGridFused_ = 0;
+  int denseGrid_ = 0;
   int runBlocksPerSM_ = 0;
   VertexData *vdHost_ = nullptr;
   EdgeData *edHost_ = nullptr;

@@ -150,6 +150,12 @@ typedef struct {
    * one phase, vertex data versioned across the two buffers */
   int32_t fused;
   uint32_t *ver;              /* [V] (stamp << 1) | buffer of the newest value */
+  /* the run starts with dense rounds (allActive): the caller may run them in
+   * a leaner kernel first, which leaves the state the main kernel resumes
+   * from in resume[4] = rounds done, vcur, dense -> list transition pending,
+   * run ended; denseFirst tells the main kernel to resume */
+  int32_t denseFirst;
+  int32_t *resume;
 } gas_run_args;
 
 /* The vertices whose apply returned true in the round just scattered, for

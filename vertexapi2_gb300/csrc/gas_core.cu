@@ -96,6 +96,7 @@ struct Ctl {
   unsigned long long dense[3][4];  // per-round counters of dense rounds (kDenseCntStride)
   unsigned err;     // device error bits (kept across set_active)
   unsigned pad;
+  int32_t resume[4];  // hand-over of a leading dense-rounds kernel (gas_run_args::resume)
 };
 
 enum DirtyBit : unsigned {
@@ -1019,6 +1020,7 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.allActive =
       (c->rangeMode && c->rstart == 0 && c->rcount == c->nV && ra.denseAlpha > 0) ? 1 : 0;
   ra.vcurOut = &c->ctl->vcur;
+  ra.resume = &c->ctl->resume[0];
 
   cudaEventRecord(c->t0, c->stream);
   st = runLaunch(user, &ra, (void *)c->stream);
