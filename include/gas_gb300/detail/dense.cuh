@@ -50,6 +50,12 @@ struct DenseCtx {
   int32_t prevStamp;       // stamp of the previous round's apply-returned-true set
   int32_t curStamp;
   int32_t allActive;       // every vertex active (setActive(0, V))
+  // Mark mode (a list round run as a pull pass): v is active iff
+  // actMark[v] == markStamp (the previous round's scatter marks); inactive
+  // vertices gather nothing.  Null: activity from the in-neighbours' stamps.
+  const int32_t *actMark;
+  int32_t markStamp;
+  int32_t skipStamps;      // allActive or mark mode: no per-edge stamp reads
   int32_t haveGather;
   int32_t iteration;
   unsigned long long *cnt;  // [3]: (active << 32 | in-edges), (ret << 32 | out-edges),
@@ -90,7 +96,7 @@ __device__ __forceinline__ void edge_step(const DenseCtx &a, int v, int e,
   typedef typename P::VertexData VD;
   const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
   const int src = __ldg(a.inSources + e);
-  x.act |= (a.allActive || a.prevRet[src] == a.prevStamp) ? 1u : 0u;
+  x.act |= (a.skipStamps || a.prevRet[src] == a.prevStamp) ? 1u : 0u;
   if (a.haveGather) {
     const typename P::GatherResult m = P::gatherMap(vd + v, vd + src, edge_ptr<P>(a.edgeData, e));
     x.val = x.has ? P::gatherReduce(x.val, m) : m;
@@ -131,7 +137,7 @@ __device__ __forceinline__ void strided_edges(const DenseCtx &a, int v, int beg,
   constexpr int J = kStrideDepth;
   const int lane = threadIdx.x & 31;
   const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
-  bool known = a.allActive != 0;  // warp-uniform
+  bool known = a.skipStamps != 0;  // warp-uniform
   for (int base = beg; base < end; base += J * 32) {
     int src[J];
 #pragma unroll
@@ -174,7 +180,7 @@ __device__ __forceinline__ void dense_finish(const DenseCtx &a, int v, unsigned 
   typedef typename P::VertexData VD;
   const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
   VD tmp = vd[v];
-  if (a.allActive || act) {
+  if (a.allActive || (a.actMark ? a.actMark[v] == a.markStamp : act != 0u)) {
     const bool r = do_apply<P>(&tmp, g, a.iteration);
     ++c.active;
     c.inEdges += (unsigned)inDeg;
@@ -185,6 +191,11 @@ __device__ __forceinline__ void dense_finish(const DenseCtx &a, int v, unsigned 
     }
   }
   reinterpret_cast<VD *>(a.vdNext)[v] = tmp;
+}
+
+// Mark mode: v is not active this round (its edges are skipped).
+__device__ __forceinline__ bool mark_inactive(const DenseCtx &a, int v) {
+  return a.actMark != nullptr && a.actMark[v] != a.markStamp;
 }
 
 // Warp work units of one dense pass: [large-vertex chunks | one vertex per
@@ -207,7 +218,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     const int ch = (int)u;
     const int v = a.chunkVertex[ch];
     const int beg = a.chunkBegin[ch];
-    const int end = min(beg + kChunkEdges, a.inOffsets[v + 1]);
+    const int end = mark_inactive(a, v) ? beg : min(beg + kChunkEdges, a.inOffsets[v + 1]);
     strided_edges<P>(a, v, beg, end, x);
     group_reduce<P, 32>(x);
     unsigned last = 0u;
@@ -256,7 +267,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
   if (u < a.nMid) {
     // ---- one vertex per warp (in-degree 65..1024)
     const int v = a.binMid[u];
-    const int beg = a.inOffsets[v], end = a.inOffsets[v + 1];
+    const int beg = a.inOffsets[v], end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
     strided_edges<P>(a, v, beg, end, x);
     group_reduce<P, 32>(x);
     if (lane == 0) dense_finish<P>(a, v, x.act, combined_result<P>(a, x), end - beg, c);
@@ -272,7 +283,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     if (idx < a.nSmall) {
       v = a.binSmall[idx];
       beg = a.inOffsets[v];
-      end = a.inOffsets[v + 1];
+      end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
     }
 #pragma unroll
     for (int k = 0; k < 64 / kSmallLanes; ++k) {
@@ -290,7 +301,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     const long long idx = u * 32 + lane;
     if (idx >= a.nTiny) return;
     const int v = a.binTiny[idx];
-    const int beg = a.inOffsets[v], end = a.inOffsets[v + 1];
+    const int beg = a.inOffsets[v], end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
     typedef typename P::VertexData VD;
     const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
     int src[GAS_TPV_MAX_DEGREE];
@@ -302,7 +313,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
 #pragma unroll
     for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k)
       if (beg + k < end) {
-        act |= (a.allActive || a.prevRet[src[k]] == a.prevStamp) ? 1u : 0u;
+        act |= (a.skipStamps || a.prevRet[src[k]] == a.prevStamp) ? 1u : 0u;
         if (a.haveGather)
           g = P::gatherReduce(g, P::gatherMap(vd + v, vd + src[k], edge_ptr<P>(a.edgeData, beg + k)));
       }

@@ -10,9 +10,13 @@
 //   -> grid barrier -> swap frontier, next round
 //
 // Rounds whose predecessor activated many out-edges run dense (pull, see
-// dense.cuh): one pass of degree-binned warp units and one barrier.  Transitions build the other
-// representation: list -> dense stamps the scatter list, dense -> list
-// compacts the stamped vertices into a scatter list and pushes it.
+// dense.cuh): one pass of degree-binned warp units and one barrier.
+// Transitions build the other representation: list -> dense stamps the
+// scatter list, dense -> list compacts the stamped vertices into a scatter
+// list and pushes it.  A list round whose frontier has many in-edges runs
+// as a pull pass too, over the vertices the previous scatter marked.  A run
+// that starts with every vertex active may run its leading dense rounds in
+// run_dense_kernel, a kernel with a smaller register budget, first.
 //
 // Tiles are assigned statically (tile t to block t mod grid, in increasing
 // order per block); all blocks are co-resident (cooperative launch), so a
@@ -101,9 +105,10 @@ __device__ __forceinline__ DenseCtx dense_ctx(const gas_run_args &ra) {
   return dc;
 }
 
-// Round r's per-round settings of a dense pass over vdBuf[vcur].
+// Round r's per-round settings of a dense pass over vdBuf[vcur]; with
+// byMark, the active vertices are those round r-1's scatter marked.
 __device__ __forceinline__ void dense_round(DenseCtx &dc, const gas_run_args &ra, void *const vdBuf[2],
-                                            int vcur, int r, bool allActive) {
+                                            int vcur, int r, bool allActive, bool byMark = false) {
   const int32_t stamp = ra.stampBase + r;
   dc.vdCur = vdBuf[vcur];
   dc.vdNext = vdBuf[vcur ^ 1];
@@ -112,6 +117,9 @@ __device__ __forceinline__ void dense_round(DenseCtx &dc, const gas_run_args &ra
   dc.prevStamp = stamp - 1;
   dc.curStamp = stamp;
   dc.allActive = allActive ? 1 : 0;
+  dc.actMark = byMark ? ra.mark : nullptr;
+  dc.markStamp = stamp - 1;
+  dc.skipStamps = (allActive || byMark) ? 1 : 0;
   dc.iteration = ra.g.iteration + r;
   dc.cnt = ra.denseCnt + kDenseCntStride * (r % 3);
 }
@@ -212,6 +220,10 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_ru
   }
 }
 
+// A list round whose frontier has more than nEdges / kMarkPullFactor in-edges
+// runs as a pull pass over the marked frontier.
+constexpr long long kMarkPullFactor = 4;
+
 // MinBlocks CTAs of 256 threads per SM: the register budget a thread gets
 // (2: 128, 3: 80, 4: 64).
 template <class P, int MinBlocks = 3>
@@ -265,17 +277,24 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
     if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, cur, sidx);
     unsigned long long statA, statR;
     bool denseNext;
+    bool byMark = false;  // a list round run as a pull pass over its marked frontier
+    int n = 0, T = 0;
     if (mode == kList) {
-      // ---------------- push round: list (or range) frontier
       a.rangeMode = rangeMode ? 1 : 0;
       a.front = ra.frontL[cur];
       a.scat = ra.scatL[sidx];
       a.epoch = epoch;
       a.iteration = ra.g.iteration + r;
       a.vertexData = vdBuf[vcur];
-      int n, T;
       frontier_size(a, n, T);
       if (n == 0) break;  // uniform: every block read the same count
+      // A frontier whose in-edges are a large share of the graph gathers
+      // faster in a pull pass that skips the unmarked vertices.
+      byMark = r > 0 && !rangeMode && !versioned && a.haveGather && ra.denseAlpha > 0 &&
+               (long long)T * kMarkPullFactor > E;
+    }
+    if (mode == kList && !byMark) {
+      // ---------------- push round: list (or range) frontier
       bool tpvG;
       const int ntG = gather_tiles(a, n, T, tpvG);
       if (ra.fused && (tpvG || !a.haveGather)) {
@@ -366,7 +385,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       }  // two-phase round
     } else {
       // ---------------- pull round over every vertex
-      dense_round(dc, ra, vdBuf, vcur, r, allActive);
+      dense_round(dc, ra, vdBuf, vcur, r, allActive, byMark);
       dense_pass<P>(dc);
       if (!grid_barrier(ra.barrier, a.errWord)) break;
       statA = dc.cnt[0];
