@@ -41,11 +41,16 @@ __device__ __forceinline__ VD fused_read(const FusedCtx &f, int v) {
   return s ? x1 : x0;
 }
 
+// Frontiers of at most this many vertices append per warp (one atomic per
+// warp, no block barrier); larger ones per block (one atomic per block).
+constexpr int kWarpAppendMax = 4096;
+
 // One tile of GAS_TPV_TILE frontier vertices.  Counts this round's
 // apply-returned-true vertices and their out-edges into cRet / cOut.
+// warpAppend (block-uniform): append the activated vertices per warp.
 template <class P>
 __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const ScatterArgs &sa, const FusedCtx &f,
-                               int t, int n, int T, ScatterSmem &sm, unsigned &cRet,
+                               int t, int n, int T, bool warpAppend, ScatterSmem &sm, unsigned &cRet,
                                unsigned &cOut) {
   typedef typename P::VertexData VD;
   typedef typename P::GatherResult GR;
@@ -122,8 +127,11 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
   }
 #pragma unroll
   for (int k = 0; k < D; ++k) dg[k] -= bg[k];
-  block_append<kSNT, D, GAS_GATHER_TILE>(ok, dst, dg, bg, sa.next, sa.maxGatherTiles, a.capacity,
-                                         a.errWord, sm.app);
+  if (warpAppend)  // the next round's consumer is one thread per entry: no split hints
+    warp_append_list<D>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
+  else
+    block_append<kSNT, D, GAS_GATHER_TILE>(ok, dst, dg, bg, sa.next, sa.maxGatherTiles, a.capacity,
+                                           a.errWord, sm.app);
 }
 
 // Every vertex's newest value into slot 0 (the run's current buffer).

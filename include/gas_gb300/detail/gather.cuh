@@ -131,9 +131,11 @@ __device__ __forceinline__ void front_entry(const gas_gather_args &a, int i, int
   }
 }
 
-// Gather tiles of the current round: mode and count.
-__device__ __forceinline__ int gather_tiles(const gas_gather_args &a, int n, int T, bool &tpv) {
-  tpv = a.haveGather && frontier_max_degree(a) <= GAS_TPV_MAX_DEGREE;
+// Gather tiles of the current round: mode and count (maxDeg: the
+// frontier's largest in-degree, frontier_max_degree).
+__device__ __forceinline__ int gather_tiles(const gas_gather_args &a, int n, int T, unsigned maxDeg,
+                                            bool &tpv) {
+  tpv = a.haveGather && maxDeg <= GAS_TPV_MAX_DEGREE;
   long long items;
   int tile;
   if (!a.haveGather) {
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(kGNT) gather_apply_kernel(const gas_gather_arg
   int n, T;
   frontier_size(a, n, T);
   bool tpv;
-  const int ntiles = gather_tiles(a, n, T, tpv);
+  const int ntiles = gather_tiles(a, n, T, frontier_max_degree(a), tpv);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *a.resetCount = 0ull;
     *a.resetMaxDeg = 0u;

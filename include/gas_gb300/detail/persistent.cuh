@@ -37,20 +37,24 @@ namespace detail {
 // ~2-4 s of polling before a grid barrier reports a timeout
 constexpr unsigned kBarrierSpinLimit = 1u << 25;
 
-// Grid-wide barrier of a cooperative launch (bar[0] arrivals, bar[1]
-// generation).  Returns false on timeout or when another block reported one.
+// Grid-wide barrier of a cooperative launch.  bar (8-byte aligned) is one
+// 64-bit word, generation << 32 | arrivals (bar[0] arrivals, bar[1]
+// generation); arrivals must be 0 at launch.  Each block adds one arrival
+// and learns the generation from the same atomic; the last arrival starts
+// the next generation and clears the arrivals with one more atomic, which
+// nothing waits on, and the others poll the generation.  Returns false on
+// timeout or when another block reported one.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
   __shared__ unsigned s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned ok = 1u;
+    unsigned long long *word = reinterpret_cast<unsigned long long *>(bar);
     __threadfence();
-    const unsigned gen = ld_acquire(bar + 1);
-    const unsigned arrived = atomicAdd(bar, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      st_release(bar + 1, gen + 1);
+    const unsigned long long old = atomicAdd(word, 1ull);
+    const unsigned gen = (unsigned)(old >> 32);
+    if ((unsigned)old == gridDim.x - 1) {
+      atomicAdd(word, (1ull << 32) - gridDim.x);
     } else {
       unsigned spins = 0;
       while (ld_acquire(bar + 1) == gen) {
@@ -279,6 +283,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
     bool denseNext;
     bool byMark = false;  // a list round run as a pull pass over its marked frontier
     int n = 0, T = 0;
+    unsigned frontMaxDeg = 0u;
     if (mode == kList) {
       a.rangeMode = rangeMode ? 1 : 0;
       a.front = ra.frontL[cur];
@@ -287,6 +292,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       a.iteration = ra.g.iteration + r;
       a.vertexData = vdBuf[vcur];
       frontier_size(a, n, T);
+      frontMaxDeg = frontier_max_degree(a);  // loaded together with the count
       if (n == 0) break;  // uniform: every block read the same count
       // A frontier whose in-edges are a large share of the graph gathers
       // faster in a pull pass that skips the unmarked vertices.
@@ -296,7 +302,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
     if (mode == kList && !byMark) {
       // ---------------- push round: list (or range) frontier
       bool tpvG;
-      const int ntG = gather_tiles(a, n, T, tpvG);
+      const int ntG = gather_tiles(a, n, T, frontMaxDeg, tpvG);
       if (ra.fused && (tpvG || !a.haveGather)) {
         // ---------------- fused round: one phase, one barrier
         FusedCtx f;
@@ -309,9 +315,10 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         sa.stamp = stamp;
         unsigned cRet = 0u, cOut = 0u;
         const int ntF = (n + GAS_TPV_TILE - 1) / GAS_TPV_TILE;
+        const bool warpAppend = n <= kWarpAppendMax;
         for (int t = blockIdx.x; t < ntF; t += gridDim.x) {
-          fused_tpv_tile<P>(a, sa, f, t, n, T, sm.s, cRet, cOut);
-          __syncthreads();
+          fused_tpv_tile<P>(a, sa, f, t, n, T, warpAppend, sm.s, cRet, cOut);
+          if (!warpAppend) __syncthreads();
         }
         cRet = __reduce_add_sync(kFullMask, cRet);
         cOut = __reduce_add_sync(kFullMask, cOut);

@@ -349,5 +349,57 @@ __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t 
   __syncthreads();
 }
 
+// warp_append: block_append for one warp, without split hints (for lists
+// whose consumer walks one thread per entry): the warp reserves its
+// (count, degree sum) with one atomicAdd on the packed counter and every
+// lane writes its own entries.  No shared memory, no block barrier.
+template <int K>
+__device__ __forceinline__ void warp_append_list(const bool (&ok)[K], const int32_t (&vid)[K],
+                                                 const int32_t (&deg)[K], const int32_t (&beg)[K],
+                                                 const gas_vertex_list &out, int32_t capacity,
+                                                 unsigned *errWord) {
+  const int lane = threadIdx.x & 31;
+  unsigned cnt = 0, esum = 0, dmax = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (ok[k]) {
+      ++cnt;
+      esum += (unsigned)deg[k];
+      dmax = max(dmax, (unsigned)deg[k]);
+    }
+  const unsigned long long mine = ((unsigned long long)cnt << 32) | esum;
+  unsigned long long incl = mine;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long o = __shfl_up_sync(kFullMask, incl, d);
+    if (lane >= d) incl += o;
+  }
+  const unsigned long long total = __shfl_sync(kFullMask, incl, 31);
+  if (total == 0ull) return;  // warp-uniform
+  const unsigned wmax = __reduce_max_sync(kFullMask, dmax);
+  unsigned long long base = 0ull;
+  if (lane == 0) {
+    base = atomicAdd(out.count, total);
+    atomicMax(out.maxDeg, wmax);
+  }
+  base = __shfl_sync(kFullMask, base, 0);
+  const unsigned long long excl = incl - mine;
+  long long q = (long long)(base >> 32) + (long long)(excl >> 32);
+  long long e = (long long)(base & 0xffffffffull) + (long long)(excl & 0xffffffffull);
+  if ((long long)(base >> 32) + (long long)(total >> 32) > capacity) {
+    if (lane == 0) atomicOr(errWord, GAS_DEVERR_CAPACITY);
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (ok[k]) {
+      out.vid[q] = vid[k];
+      out.pre[q] = (int32_t)e;
+      out.beg[q] = beg[k];
+      ++q;
+      e += deg[k];
+    }
+}
+
 }  // namespace detail
 }  // namespace gas

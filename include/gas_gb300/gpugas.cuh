@@ -207,10 +207,7 @@ class EngineGPU {
   static constexpr int kRunBlocksPerSM = 4;
   // A run that starts with every vertex active runs its leading dense rounds
   // in run_dense_kernel (40 registers, 6 CTAs per SM), then resumes here.
-#ifndef GAS_DENSE_BLOCKS_PER_SM
-#define GAS_DENSE_BLOCKS_PER_SM 6
-#endif
-  static constexpr int kDenseBlocksPerSM = GAS_DENSE_BLOCKS_PER_SM;
+  static constexpr int kDenseBlocksPerSM = 6;
 
   static gas_status launchRun(void *user, const gas_run_args *ra, void *stream) {
     EngineGPU *self = static_cast<EngineGPU *>(user);
