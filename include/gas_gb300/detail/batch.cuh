@@ -394,7 +394,7 @@ __device__ __forceinline__ void warp_append_pair(bool want, uint32_t entry, uint
 // edges together, up to the warp's largest out-degree).
 template <int W, int KIND>
 __device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, uint32_t entry,
-                                                int round, unsigned *nxt, uint32_t *listNext,
+                                                int round, unsigned *cur, unsigned *nxt, uint32_t *listNext,
                                                 unsigned long long *cntNext,
                                                 unsigned long long &changed,
                                                 const BatchBucket bk) {
@@ -409,6 +409,11 @@ __device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, 
   int du = 0;
   bool keep = false;
   if (KIND == kBatchSSSP && valid) {
+    // Every bit of this round's mask belongs to a pair of this round's
+    // list, and nothing else touches the mask this round: each pair clears
+    // its word (idempotent zeros), so the mask is clean when it next
+    // collects pairs, without a pass over all vertices.
+    cur[(size_t)u * W + wq] = 0u;
     du = __ldcg(a.value + (size_t)u * Q + q);
     if (bk.bound && du >= bk.bound[q]) {  // not this bucket: keep (u, q) for later
       const unsigned old = atomicOr(nxt + (size_t)u * W + wq, bit);
@@ -497,7 +502,7 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       if (blockIdx.x == 0 && threadIdx.x < W) a.nearFlag[(r + 1) % 3][threadIdx.x] = 0u;
       __syncthreads();
     }
-    const unsigned *cur = a.mask[r % 3];
+    unsigned *cur = a.mask[r % 3];
     unsigned *nxt = a.mask[(r + 1) % 3];
     unsigned *clr = a.mask[(r + 2) % 3];
     const int rc = r % 3, rn = (r + 1) % 3;
@@ -514,9 +519,10 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       a.cnt[rn] = 0ull;
       a.listCnt[(r + 2) % 3] = 0ull;  // input of round r-1, appended in round r+1
     }
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
-         i += (size_t)gridDim.x * blockDim.x)
-      clr[i] = 0u;
+    if (!a.pairMode)  // pair rounds clear their own mask words (batch_pair_unit)
+      for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
+           i += (size_t)gridDim.x * blockDim.x)
+        clr[i] = 0u;
     unsigned long long changed = 0ull;
     if (a.pairMode) {
       const uint32_t *pc = a.pairs[rc];
@@ -525,8 +531,8 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       for (long long base = gw * 32; base < nList; base += threads) {
         const long long i = base + (threadIdx.x & 31);
         const bool valid = i < nList;
-        batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, nxt, pn, cntNext,
-                                 changed, bk);
+        batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, cur, nxt,
+                                 pn, cntNext, changed, bk);
       }
     } else if (push) {
       for (long long i = gw; i < nList; i += warps)

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int
     if (blockIdx.x == 0 && threadIdx.x < W) a.nearFlag[rn][threadIdx.x] = 0u;
     __syncthreads();
   }
-  const unsigned *cur = a.mask[rc];
+  unsigned *cur = a.mask[rc];
   unsigned *nxt = a.mask[rn];
   unsigned *clr = a.mask[(r + 2) % 3];
   const unsigned long long lc = a.listCnt[rc];
@@ -73,9 +73,10 @@ __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int
     a.cnt[rn] = 0ull;
     a.listCnt[(r + 2) % 3] = 0ull;
   }
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
-       i += (size_t)gridDim.x * blockDim.x)
-    clr[i] = 0u;
+  if (!a.pairMode)  // pair rounds clear their own mask words (batch_pair_unit)
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
+         i += (size_t)gridDim.x * blockDim.x)
+      clr[i] = 0u;
   unsigned long long changed = 0ull;
   if (a.pairMode) {
     const uint32_t *pc = a.pairs[rc];
@@ -84,8 +85,8 @@ __global__ void __launch_bounds__(256) batch_round_kernel(const BatchArgs a, int
     for (long long base = gw * 32; base < nList; base += threads) {
       const long long i = base + (threadIdx.x & 31);
       const bool valid = i < nList;
-      batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, nxt, pn, a.listCnt + rn,
-                               changed, bk);
+      batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, cur, nxt,
+                               pn, a.listCnt + rn, changed, bk);
     }
   } else if (push) {
     for (long long i = gw; i < nList; i += warps)

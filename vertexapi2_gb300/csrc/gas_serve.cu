@@ -40,6 +40,7 @@ constexpr int kPprRounds = 20;    // PPR iterations (a fixed count, as run(20))
 constexpr int kFirstChunk = 4;    // rounds queued per chunk: 4, 8, ... 64
 constexpr int kMaxChunk = 64;
 constexpr int kKinds = 3;         // BFS, SSSP, PPR
+constexpr int64_t kTieNs = 20000000;  // queries this close in arrival count as a burst
 
 // Makes `device` current for the scope and restores the caller's device.
 struct DeviceGuard {
@@ -123,11 +124,13 @@ struct Batch {
   gas::detail::BatchArgs ba;
   gas::detail::PprArgs pa;
   bool pairs = false;             // (vertex, query) pair frontier
+  int64_t pairsSeen = 0;          // largest pair list seen at a chunk's end
   int32_t delta = 0;              // SSSP distance buckets
   int roundsIssued = 0;
   int chunk = kFirstChunk;
   int unfetched = 0;
   int64_t admitNs = 0;
+  size_t cell = 0;                 // graph * kKinds + kind
   cudaStream_t stream = nullptr;
   class Server *server = nullptr;
   ~Batch();
@@ -142,6 +145,11 @@ struct ChunkMark {  // a queued end test: event + pinned copy of the control wor
 
 struct Lane {
   cudaStream_t stream = nullptr;
+  // Batches on graphs of many rounds (the pair-frontier graphs: low degree,
+  // high diameter) run on a high-priority stream: each of their rounds is a
+  // small kernel, and under load they would otherwise queue behind the
+  // large round kernels of other lanes, round after round.
+  cudaStream_t streamHi = nullptr;
   std::shared_ptr<Batch> batch;
   ChunkMark marks[3];
   std::deque<int> queued;  // indices of marks in flight, in issue order
@@ -163,6 +171,7 @@ class Server {
   std::condition_variable cvWork, cvDone;
   std::map<uint64_t, Query *> queries;
   std::vector<std::deque<Query *>> pending;  // per graph * kinds
+  std::vector<int64_t> cellRunNs;            // recent batch run time per graph * kinds
   std::vector<ServeGraph *> graphs;
   uint64_t nextTicket = 1;
   gas_server_stats stats;
@@ -242,8 +251,12 @@ gas_status Server::start() {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&fetch, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost(&mirrors, sizeof(Ctl) * 3 * cfg.lanes);
   if (e == cudaSuccess) e = cudaMallocHost(&srcPinned, sizeof(int32_t) * kMaxQ * cfg.lanes);
+  int leastPri = 0, greatestPri = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&leastPri, &greatestPri);
   for (int l = 0; l < cfg.lanes && e == cudaSuccess; ++l) {
     e = cudaStreamCreateWithFlags(&lanes[l].stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+      e = cudaStreamCreateWithPriority(&lanes[l].streamHi, cudaStreamNonBlocking, greatestPri);
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
       e = cudaEventCreateWithFlags(&lanes[l].marks[k].ev, cudaEventDisableTiming);
       lanes[l].marks[k].mirror = mirrors + 3 * l + k;
@@ -266,6 +279,7 @@ Server::~Server() {
   for (int l = 0; l < kMaxLanes; ++l) {
     Lane &L = lanes[l];
     if (L.stream) cudaStreamSynchronize(L.stream);
+    if (L.streamHi) cudaStreamSynchronize(L.streamHi);
     L.batch.reset();
     for (auto &m : L.marks)
       if (m.ev) cudaEventDestroy(m.ev);
@@ -280,8 +294,10 @@ Server::~Server() {
   queries.clear();
   for (int32_t *p : toFree) cudaFreeAsync(p, fetch);
   if (fetch) cudaStreamSynchronize(fetch);
-  for (int l = 0; l < kMaxLanes; ++l)
+  for (int l = 0; l < kMaxLanes; ++l) {
     if (lanes[l].stream) cudaStreamDestroy(lanes[l].stream);
+    if (lanes[l].streamHi) cudaStreamDestroy(lanes[l].streamHi);
+  }
   if (fetch) cudaStreamDestroy(fetch);
   for (ServeGraph *g : graphs) {
     if (!g) continue;
@@ -302,7 +318,9 @@ template <int W, int KIND>
 void round_pair(const gas::detail::BatchArgs &a, int r, unsigned *done, int blocks,
                 cudaStream_t s) {
   gas::detail::batch_round_kernel<W, KIND><<<blocks, 256, 0, s>>>(a, r, done);
-  gas::detail::batch_tail_kernel<W><<<blocks, 256, 0, s>>>(a, r, done);
+  // push-only batches (pairs, buckets): the tail is the end test alone
+  const int tailBlocks = (a.pairMode || a.delta > 0) ? 1 : blocks;
+  gas::detail::batch_tail_kernel<W><<<tailBlocks, 256, 0, s>>>(a, r, done);
 }
 
 template <int QP>
@@ -381,7 +399,14 @@ void Server::issue_chunk(int l, int rounds, bool final) {
     b.roundsIssued += rounds;
     launches += rounds;
   } else {
-    const int blocks = round_blocks(*this, std::max<int64_t>(b.g->bg.nUnits, V));
+    int blocks = round_blocks(*this, std::max<int64_t>(b.g->bg.nUnits, V));
+    if (b.pairs) {
+      // pair rounds walk the pair list only: a grid for about twice the
+      // largest list seen so far (the rounds grid-stride past it), so that
+      // a small batch's rounds need few block slots on a busy device
+      const int64_t want = (2 * std::max<int64_t>(b.pairsSeen, b.nQ) + 512LL * b.nQ + 255) / 256;
+      blocks = (int)std::max<int64_t>(1, std::min<int64_t>(blocks, want));
+    }
     for (int k = 0; k < rounds; ++k) enqueue_round(b, b.roundsIssued + k, blocks);
     b.roundsIssued += rounds;
     launches += 2 * rounds;
@@ -400,7 +425,7 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
   Batch &b = *bp;
   Lane &L = lanes[l];
   b.lane = l;
-  b.stream = L.stream;
+  b.stream = b.pairs ? L.streamHi : L.stream;
   const ServeGraph &g = *b.g;
   const int32_t V = g.bg.g.nV;
   const size_t Vs = (size_t)std::max(V, 1);
@@ -552,6 +577,11 @@ void Server::finish_batch(int l, gas_status st, int32_t rounds) {
       if (st == GAS_OK) ++stats.completed; else ++stats.failed;
     }
     --stats.running;
+    if (st == GAS_OK) {
+      int64_t &c = cellRunNs[b.cell];
+      const int64_t d = t - b.admitNs;
+      c = c == 0 ? d : (3 * c + d) / 4;
+    }
   }
   L.batch.reset();
   L.queued.clear();
@@ -574,6 +604,7 @@ bool Server::poll_lane(int l) {
   m.busy = false;
   Batch &b = *L.batch;
   const Ctl c = *m.mirror;
+  for (int k = 0; k < 3; ++k) b.pairsSeen = std::max<int64_t>(b.pairsSeen, (int64_t)(c.listCnt[k] >> 32));
   if (m.final) {
     finish_batch(l, c.err ? GAS_ERR_TIMEOUT : GAS_OK, b.kind == 2 ? kPprRounds : c.rounds);
     return true;
@@ -591,8 +622,11 @@ bool Server::poll_lane(int l) {
   return true;
 }
 
-// Starts batches on free lanes: the (graph, program) queue holding the
-// oldest waiting query first, as many of its queries as memory admits.
+// Starts batches on free lanes, as many queries of one (graph, program)
+// queue as memory admits.  The queue holding the oldest waiting query goes
+// first -- except among queues whose oldest queries arrived within
+// kTieNs of it (a burst), where the one with the longest recent batch run
+// time goes first, so that the longest batches do not start last.
 bool Server::admit() {
   bool any = false;
   {
@@ -604,13 +638,21 @@ bool Server::admit() {
     std::shared_ptr<Batch> bp;
     {
       std::lock_guard<std::mutex> lk(mu);
-      int best = -1;
-      int64_t bestT = 0;
+      int64_t oldest = 0;
+      bool anyPending = false;
       for (size_t i = 0; i < pending.size(); ++i)
-        if (!pending[i].empty() && (best < 0 || pending[i].front()->info.submitNs < bestT)) {
-          best = (int)i;
-          bestT = pending[i].front()->info.submitNs;
+        if (!pending[i].empty() && (!anyPending || pending[i].front()->info.submitNs < oldest)) {
+          oldest = pending[i].front()->info.submitNs;
+          anyPending = true;
         }
+      int best = -1;
+      for (size_t i = 0; anyPending && i < pending.size(); ++i) {
+        if (pending[i].empty() || pending[i].front()->info.submitNs > oldest + kTieNs) continue;
+        if (best < 0 || cellRunNs[i] > cellRunNs[best] ||
+            (cellRunNs[i] == cellRunNs[best] &&
+             pending[i].front()->info.submitNs < pending[best].front()->info.submitNs))
+          best = (int)i;
+      }
       if (best < 0) return any;
       std::deque<Query *> &pq = pending[best];
       ServeGraph *g = graphs[best / kKinds];
@@ -647,6 +689,7 @@ bool Server::admit() {
       bp = std::make_shared<Batch>();
       bp->g = g;
       bp->kind = kind;
+      bp->cell = (size_t)best;
       bp->nQ = nQ;
       bp->Q = row_width(kind, nQ);
       bp->W = std::max(bp->Q / 32, 1);
@@ -881,6 +924,7 @@ gas_status gas_server_add_graph(gas_server *h, int32_t nVertices, int32_t nEdges
   g->id = (int32_t)s.graphs.size();
   s.graphs.push_back(g);
   s.pending.resize(s.graphs.size() * kKinds);
+  s.cellRunNs.resize(s.graphs.size() * kKinds, 0);
   *graphId = g->id;
   return GAS_OK;
 }
