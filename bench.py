@@ -733,21 +733,35 @@ def serve_summary(infos, gs=None):
            "mean_batch": float(np.mean([x["batchSize"] for x in infos]))}
     if gs is not None:  # p50 latency and rounds per graph and program
         names = {1: "bfs", 2: "sssp", 5: "ppr"}
-        cells = {}
+        cells, batches = {}, {}
         for x, l in zip(infos, lat):
-            cells.setdefault(f"{gs[x['graph']][0]}-{names[x['program']]}", []).append(
-                (l, x["rounds"], (x["doneNs"] - x["admitNs"]) / 1e6))
+            key = f"{gs[x['graph']][0]}-{names[x['program']]}"
+            cells.setdefault(key, []).append((l, x["rounds"], (x["doneNs"] - x["admitNs"]) / 1e6))
+            batches.setdefault(key, {})[(x["lane"], x["admitNs"])] = (x["doneNs"] - x["admitNs"]) / 1e6
+        # lane_ms: the cell's batches' run times summed (lane time it held)
         out["cells"] = {k: {"n": len(v), "p50_ms": float(np.median([a for a, _, _ in v])),
                             "run_ms": float(np.median([c for _, _, c in v])),
-                            "rounds": int(np.median([b for _, b, _ in v]))}
+                            "rounds": int(np.median([b for _, b, _ in v])),
+                            "batches": len(batches[k]), "lane_ms": float(sum(batches[k].values()))}
                         for k, v in sorted(cells.items())}
     return out
 
 
-def plain_one_at_a_time(gs, local, stream, per_cell=2):
+def pinned_like(a):
+    """A page-locked copy of the numpy array `a` (same dtype and shape)."""
+    import torch
+    buf = torch.empty(max(a.nbytes, 1), dtype=torch.uint8).pin_memory().numpy()
+    out = buf[:a.nbytes].view(a.dtype).reshape(a.shape)
+    out[...] = a
+    return out
+
+
+def plain_one_at_a_time(gs, local, stream, per_cell=4):
     """Mean run()+getResults() time of the plain engine per (graph, program)
     on `per_cell` seeded sources, the result of each, and the mix's
-    queries/s (1 / expected time per query)."""
+    queries/s (1 / expected time per query).  Initial values go up from, and
+    results come back into, page-locked host buffers, as the served queries'
+    results do."""
     import vertexapi2_gb300 as gas
     from vertexapi2_gb300 import programs as P
     from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
@@ -765,8 +779,9 @@ def plain_one_at_a_time(gs, local, stream, per_cell=2):
                     vd, act = P.sssp_init(g.n_vertices, s0), (0, g.n_vertices)
                 else:
                     vd, act = P.ppr_init(g.n_vertices, g.srcs, s0), (0, g.n_vertices)
-                if q == 0:
-                    e.set_graph(g.n_vertices, vd, g.srcs, g.dsts,
+                vd = pinned_like(vd)
+                if q == 0:  # the engine borrows a page-locked result array
+                    e.set_graph(g.n_vertices, pinned_like(vd), g.srcs, g.dsts,
                                 g.weights if prog == PROGRAM_SSSP else None)
                 else:
                     e.set_vertex_data(vd)
@@ -811,7 +826,7 @@ def run_serve_c5(args):
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             infos, wall = serve_pass(srv, ids, gs, queries, float("inf"), bufs, SEED + 100 + k)
-            steps.append((serve_summary(infos), wall))
+            steps.append((serve_summary(infos, gs if k == 0 else None), wall))
     launches = srv.stats()["kernelLaunches"] - l0
     span = allreduce_max(world, float(sum(x["span_s"] for x, _ in steps)))
     e2e_s = allreduce_max(world, float(sum(w for _, w in steps)))
@@ -871,6 +886,7 @@ def run_serve_c5(args):
         "latency_ms": {"p50": last["p50_ms"], "p99": last["p99_ms"], "at": "capacity (burst)"},
         "sweep": sweep,
         "mean_batch": last["mean_batch"],
+        "capacity_cells": steps[0][0].get("cells"),
         "alone_served_ms": {k: [float(np.mean([a for a, _ in v])), int(v[0][1])]
                             for k, v in sorted(alone.items())},
         "plain_ms": {f"{gs[k][0]}-{ {1: 'bfs', 2: 'sssp', 5: 'ppr'}[p] }": 1e3 * t

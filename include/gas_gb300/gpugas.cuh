@@ -85,10 +85,15 @@ class EngineGPU {
     if (vertexData) note(gas_core_upload_vertex_data(core_, vertexData));
   }
 
-  // gpugas.h:329-338
+  // gpugas.h:329-338.  Edge data changes only through Program::scatter
+  // (scatterEdges); without it the device copy still equals what setGraph
+  // read from the caller's edge array, so it is not copied back (on R-MAT-22
+  // that copy is 0.5 GB, 10 ms).
   void getResults() {
     if (vdHost_ && !note(gas_core_download_vertex_data(core_, vdHost_))) return;
-    if (edHost_ && kEdgeBytes) note(gas_core_download_edge_data(core_, edHost_));
+    if constexpr (kScatterEdges) {
+      if (edHost_ && kEdgeBytes) note(gas_core_download_edge_data(core_, edHost_));
+    }
   }
 
   // gpugas.h:342-349

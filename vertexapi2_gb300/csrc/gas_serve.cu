@@ -41,6 +41,8 @@ constexpr int kFirstChunk = 4;    // rounds queued per chunk: 4, 8, ... 64
 constexpr int kMaxChunk = 64;
 constexpr int kKinds = 3;         // BFS, SSSP, PPR
 constexpr int64_t kTieNs = 20000000;  // queries this close in arrival count as a burst
+constexpr int64_t kWindowDiv = 32;         // batching window: recent run time / kWindowDiv
+constexpr int64_t kWindowMaxNs = 10000000;
 
 // Makes `device` current for the scope and restores the caller's device.
 struct DeviceGuard {
@@ -623,10 +625,14 @@ bool Server::poll_lane(int l) {
 }
 
 // Starts batches on free lanes, as many queries of one (graph, program)
-// queue as memory admits.  The queue holding the oldest waiting query goes
-// first -- except among queues whose oldest queries arrived within
-// kTieNs of it (a burst), where the one with the longest recent batch run
-// time goes first, so that the longest batches do not start last.
+// queue as memory admits.  A queue is ready once it holds a full batch or
+// its oldest query has waited 1/kWindowDiv of the queue's recent batch run
+// time (at most kWindowMaxNs): a queue whose batches run long collects the
+// queries of a burst into one batch instead of starting one batch per
+// arrival.  Of the ready queues, the one holding the oldest query goes
+// first -- except among queues whose oldest queries arrived within kTieNs
+// of it (a burst), where the one with the longest recent batch run time
+// goes first, so that the longest batches do not start last.
 bool Server::admit() {
   bool any = false;
   {
@@ -638,16 +644,23 @@ bool Server::admit() {
     std::shared_ptr<Batch> bp;
     {
       std::lock_guard<std::mutex> lk(mu);
+      const int64_t tNow = now_ns();
+      auto ready = [&](size_t i) {
+        if (pending[i].empty()) return false;
+        const int64_t window = std::min(cellRunNs[i] / kWindowDiv, kWindowMaxNs);
+        return (int64_t)pending[i].size() >= cfg.maxBatch ||
+               tNow - pending[i].front()->info.submitNs >= window;
+      };
       int64_t oldest = 0;
-      bool anyPending = false;
+      bool anyReady = false;
       for (size_t i = 0; i < pending.size(); ++i)
-        if (!pending[i].empty() && (!anyPending || pending[i].front()->info.submitNs < oldest)) {
+        if (ready(i) && (!anyReady || pending[i].front()->info.submitNs < oldest)) {
           oldest = pending[i].front()->info.submitNs;
-          anyPending = true;
+          anyReady = true;
         }
       int best = -1;
-      for (size_t i = 0; anyPending && i < pending.size(); ++i) {
-        if (pending[i].empty() || pending[i].front()->info.submitNs > oldest + kTieNs) continue;
+      for (size_t i = 0; anyReady && i < pending.size(); ++i) {
+        if (!ready(i) || pending[i].front()->info.submitNs > oldest + kTieNs) continue;
         if (best < 0 || cellRunNs[i] > cellRunNs[best] ||
             (cellRunNs[i] == cellRunNs[best] &&
              pending[i].front()->info.submitNs < pending[best].front()->info.submitNs))
@@ -754,7 +767,12 @@ void Server::loop() {
     } else {
       bool waiting = false;
       for (auto &pq : pending) waiting = waiting || !pq.empty();
-      if (!waiting && !stop) cvWork.wait_for(lk, std::chrono::milliseconds(2));
+      if (!waiting && !stop) {
+        cvWork.wait_for(lk, std::chrono::milliseconds(2));
+      } else if (waiting) {  // queries inside their batching window
+        lk.unlock();
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+      }
     }
   }
 }
