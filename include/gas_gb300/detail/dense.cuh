@@ -381,6 +381,16 @@ __device__ void compact_ret(const int32_t *retStamp, int32_t stamp, const int32_
   }
 }
 
+// compact_ret as a kernel of its own (a frontier left as stamps by a run
+// that stopped before a dense round, turned into a list when needed).
+static __global__ void __launch_bounds__(256) compact_ret_kernel(const int32_t *retStamp, int32_t stamp,
+                                                                 const int32_t *outOffsets, int32_t nVertices,
+                                                                 gas_vertex_list out, int32_t maxSplit,
+                                                                 unsigned *errWord) {
+  __shared__ AppendSmem<256, 1> sm;
+  compact_ret<256, 1>(retStamp, stamp, outOffsets, nVertices, out, maxSplit, errWord, sm);
+}
+
 // List -> dense transition: stamp the vertices of a scatter list.
 __device__ __forceinline__ void stamp_list(const gas_vertex_list &l, int n, int32_t *retStamp,
                                            int32_t stamp) {

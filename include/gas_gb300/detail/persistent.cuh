@@ -177,8 +177,9 @@ __device__ __forceinline__ bool dense_to_list(const gas_run_args &ra, const gas_
 // The leading dense rounds of a run that starts with every vertex active,
 // in a kernel that holds nothing else: 40 registers a thread, 6 CTAs per SM
 // (the main kernel's list-round code needs 64 or more).  It stops before
-// the first list round and leaves ra.resume for the main kernel; the
-// rounds, stamps, resets and statistics are the main kernel's own.
+// the first list round and leaves ra.resume for the main kernel (resume[3]:
+// 0 go on, 1 the run is over, 2 stopped at maxRounds before a dense round);
+// the rounds, stamps, resets and statistics are the main kernel's own.
 template <class P, int MinBlocks>
 __global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_run_args ra) {
   DenseCtx dc = dense_ctx(ra);
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_ru
   int vcur = 0, r = 0, pending = 0, ended = 0;
   for (;;) {
     if (ra.maxRounds > 0 && r >= ra.maxRounds) {
-      ended = 1;
+      ended = 2;  // stopped before a dense round: its frontier is round r-1's stamps
       break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, ra.cur ^ (r & 1), ra.sidx ^ (r & 1));
@@ -263,10 +264,12 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   bool allActive = ra.allActive != 0;
   int r = 0;
   bool ended = false;
+  bool denseEnd = false;  // stopped at maxRounds before a dense round
   if (ra.denseFirst) {  // resume after run_dense_kernel's rounds
     r = ra.resume[0];
     vcur = ra.resume[1];
     ended = ra.resume[3] != 0;
+    denseEnd = ra.resume[3] == 2;
     cur = ra.cur ^ (r & 1);
     sidx = ra.sidx ^ (r & 1);
     mode = kList;
@@ -275,7 +278,11 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
     if (ra.resume[2] && !ended && !dense_to_list<P>(ra, a, sa, sm, r - 1, cur ^ 1, sidx ^ 1)) ended = true;
   }
   for (;;) {
-    if (ended || (ra.maxRounds > 0 && r >= ra.maxRounds)) break;
+    if (ended) break;
+    if (ra.maxRounds > 0 && r >= ra.maxRounds) {
+      denseEnd = mode == kDense;
+      break;
+    }
     const unsigned epoch = ra.epochBase + (unsigned)r;
     const int32_t stamp = ra.stampBase + r;
     if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, cur, sidx);
@@ -428,6 +435,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *ra.roundsOut = r;
     if (ra.vcurOut) *ra.vcurOut = vcur;
+    if (ra.denseEndOut) *ra.denseEndOut = denseEnd ? 1 : 0;
   }
 }
 

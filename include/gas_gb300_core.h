@@ -156,6 +156,10 @@ typedef struct {
    * run ended; denseFirst tells the main kernel to resume */
   int32_t denseFirst;
   int32_t *resume;
+  /* set to 1 when the run stopped at maxRounds before a dense round: the
+   * next frontier is then the vertices its last round stamped (retStamp)
+   * instead of a list */
+  int32_t *denseEndOut;
 } gas_run_args;
 
 /* The vertices whose apply returned true in the round just scattered, for

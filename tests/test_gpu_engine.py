@@ -289,10 +289,12 @@ def _run_policy(program, nv, s, d, init, w=None, active=None, alpha=10, max_iter
     return vd, rounds, st
 
 
-@pytest.mark.parametrize("alpha", [0, 10, 1000])
+@pytest.mark.parametrize("alpha", [0, 1, 10, 1000])
 def test_dense_policy_does_not_change_results(gpu, port, alpha):
     """Dense (pull) rounds, list (push) rounds and every mix of the two give
-    identical results and identical per-round frontier counts."""
+    identical results and identical per-round frontier counts.  alpha = 1
+    keeps most rounds in list mode, so list rounds whose frontiers hold more
+    than E/4 in-edges run as pull passes over the marked vertices."""
     g = graphs.rmat(14, 16, seed=31, symmetrize=True, weights=(1, 255))
     nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
     src = P.max_outdegree_vertex(nv, s)
@@ -399,3 +401,89 @@ def test_fused_rounds_match_two_phase_rounds(gpu, port, program):
         assert np.array_equal(a, port.sssp(nv, s, d, w, 0)[0])
     if program == PROGRAM_BFS:
         assert np.array_equal(a, port.bfs(nv, s, d, 5)[0])
+
+
+@pytest.mark.parametrize("program", [PROGRAM_CC, PROGRAM_SSSP, PROGRAM_PAGERANK])
+def test_dense_kernel_handover_at_every_round(gpu, program):
+    """A run that starts with every vertex active runs its leading dense
+    rounds in run_dense_kernel and resumes in the main kernel.  run(k) for
+    every k up to the end equals k rounds of the stepwise API (one launch per
+    phase, no dense rounds): the hand-over is right whether the dense kernel
+    stops at maxIters, at a dense -> list transition or at the end."""
+    g = graphs.rmat(13, 16, seed=41, symmetrize=program != PROGRAM_PAGERANK, weights=(1, 255))
+    nv, s, d = g.n_vertices, g.srcs, g.dsts
+    w = g.weights if program == PROGRAM_SSSP else None
+    if program == PROGRAM_CC:
+        init = P.cc_init(nv)
+    elif program == PROGRAM_SSSP:
+        init = P.sssp_init(nv, 0)
+    else:
+        init = P.pagerank_init(nv, s)
+    _, total, _ = _run_policy(program, nv, s, d, init, w=w, max_iters=12)
+    for k in range(1, total + 1):
+        vd = init.copy()
+        with GASEngine(program) as e:
+            e.set_graph(nv, vd, s, d, w)
+            e.set_active(0, nv)
+            for _ in range(k):
+                if not e.count_active():
+                    break
+                e.gather_apply()
+                e.scatter_activate()
+                e.next_iter()
+            e.get_results()
+        got, rounds, _ = _run_policy(program, nv, s, d, init, w=w, max_iters=k)
+        assert rounds == k
+        if program == PROGRAM_PAGERANK:
+            assert rel_l1(got["rank"], vd["rank"]) <= PR_REL_L1, k
+        else:
+            assert np.array_equal(got, vd), k
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_run_resumes_across_calls(gpu, port, k):
+    """run(k) called repeatedly continues where the last call stopped --
+    also when a call stops before a dense round, whose frontier exists only
+    as round stamps until the next call turns it into a list (k = 1 stops
+    before every dense round).  The dense-rounds kernel only leads a run
+    that starts with every vertex active."""
+    g = graphs.rmat(13, 16, seed=43, symmetrize=True, weights=(1, 255))
+    nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
+    for program in (PROGRAM_SSSP, PROGRAM_CC):
+        if program == PROGRAM_SSSP:
+            ref, st = port.sssp(nv, s, d, w, 0)
+            vd, ed = P.sssp_init(nv, 0), w
+        else:
+            ref, st = port.cc(nv, s, d)
+            vd, ed = P.cc_init(nv), None
+        with GASEngine(program) as e:
+            e.set_graph(nv, vd, s, d, ed)
+            e.set_active(0, nv)
+            done = 0
+            while True:
+                r = e.run(k)
+                done += r
+                if r < k:
+                    break
+            e.get_results()
+        assert np.array_equal(vd, ref) and done == st["iterations"], program
+
+
+def test_stepwise_after_run_stopped_before_dense_round(gpu, port):
+    """The stepwise API picks up a frontier a run left as round stamps."""
+    g = graphs.rmat(13, 16, seed=44, symmetrize=True, weights=(1, 255))
+    nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
+    ref, st = port.sssp(nv, s, d, w, 0)
+    for k in range(1, st["iterations"]):
+        vd = P.sssp_init(nv, 0)
+        with GASEngine(PROGRAM_SSSP) as e:
+            e.set_graph(nv, vd, s, d, w)
+            e.set_active(0, nv)
+            done = e.run(k)
+            while e.count_active():
+                e.gather_apply()
+                e.scatter_activate()
+                e.next_iter()
+                done += 1
+            e.get_results()
+        assert np.array_equal(vd, ref) and done == st["iterations"], k

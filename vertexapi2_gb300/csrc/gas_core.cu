@@ -93,6 +93,8 @@ struct Ctl {
   unsigned bar[2];  // persistent-kernel grid barrier: arrivals, generation
   int32_t rounds;   // rounds executed by the last persistent run
   int32_t vcur;     // 1 when that run's result is in the alternate buffer
+  int32_t denseEnd; // 1 when that run stopped before a dense round (gas_run_args::denseEndOut)
+  int32_t pad0;
   unsigned long long dense[3][4];  // per-round counters of dense rounds (kDenseCntStride)
   unsigned err;     // device error bits (kept across set_active)
   unsigned pad;
@@ -167,6 +169,13 @@ struct gas_core_s {
   bool haveScatList = false;
   bool countValid = false;
   int32_t countCache = 0;
+  // A persistent run that stopped at maxIters before a dense round leaves
+  // its next frontier as the vertices stamped densePendStamp in
+  // retStamp[densePendArr]; materialize() turns it into a list when a later
+  // call needs one.
+  bool densePending = false;
+  int32_t densePendStamp = 0;
+  int densePendArr = 0;
   unsigned dirty = 0;
   unsigned epoch = 0;
   int32_t stamp = 0;
@@ -270,6 +279,55 @@ gas_vertex_list scat_list(gas_core *c, int k) {
   l.count = &c->ctl->s[k].cnt;
   l.maxDeg = &c->ctl->s[k].maxd;
   return l;
+}
+
+// A frontier left as round stamps (densePending) becomes the list f[cur]:
+// the stamped vertices are compacted into s[sidx] and pushed, as the
+// persistent kernel's dense -> list transition does.
+gas_status materialize(gas_core *c) {
+  if (!c->densePending) return GAS_OK;
+  c->densePending = false;
+  gas_status st = clean(c, sbit(c->sidx) | fbit(c->cur) | kT0 | kT1);
+  if (st) return st;
+  gas::detail::compact_ret_kernel<<<c->scatterGrid, 256, 0, c->stream>>>(
+      c->retStamp[c->densePendArr], c->densePendStamp, c->outOff, c->nV, scat_list(c, c->sidx),
+      c->maxScatTiles, &c->ctl->err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "frontier compaction launch");
+  if (++c->stamp == 0x7fffffff) {
+    cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream);
+    c->stamp = 1;
+  }
+  gas::detail::ScatterArgs a;
+  memset(&a, 0, sizeof(a));
+  a.outOffsets = c->outOff;
+  a.outDests = c->outDst;
+  a.inOffsets = c->inOff;
+  a.scat = scat_list(c, c->sidx);
+  a.commit = 0;
+  a.vertexBytes = c->vertexBytes;
+  a.vertexData = c->vd;
+  a.vertexNew = c->vnew;
+  a.next = front_list(c, c->cur);
+  a.maxGatherTiles = c->maxGatherTiles;
+  a.capacity = c->nV;
+  a.mark = c->mark;
+  a.stamp = c->stamp;
+  a.tileCounter = &c->ctl->tile[1];
+  a.resetTile = &c->ctl->tile[0];
+  a.resetScatCount = &c->ctl->s[c->sidx ^ 1].cnt;
+  a.resetScatMaxDeg = &c->ctl->s[c->sidx ^ 1].maxd;
+  a.errWord = &c->ctl->err;
+  gas::detail::scatter_activate_kernel<<<c->scatterGrid, gas::detail::kSNT, 0, c->stream>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "frontier push launch");
+  c->dirty |= sbit(c->sidx) | kT1;
+  c->dirty &= ~(fbit(c->cur) | kT0 | sbit(c->sidx ^ 1));
+  c->rangeMode = false;
+  c->countValid = false;
+  c->pendingCommit = false;
+  c->haveScatList = false;
+  return GAS_OK;
 }
 
 gas_status check_device_error(gas_core *c) {
@@ -600,6 +658,7 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   }
   c->haveGraph = true;
   c->dirty = 0;
+  c->densePending = false;
   c->epoch = 0;
   c->stamp = 0;
   c->iteration = 0;
@@ -670,6 +729,7 @@ gas_status gas_core_set_active(gas_core *c, int32_t start, int32_t end) {
   cudaError_t e = cudaMemsetAsync(c->ctl, 0, offsetof(Ctl, err), c->stream);  // keep err
   if (e != cudaSuccess) return cuda_fail(e, "set_active reset");
   c->dirty = 0;
+  c->densePending = false;
   c->rangeMode = true;
   c->rstart = start;
   c->rcount = end - start;
@@ -694,6 +754,11 @@ gas_status gas_core_set_active(gas_core *c, int32_t start, int32_t end) {
 gas_status gas_core_count_active(gas_core *c, int32_t *n) {
   if (!c || !n) return fail(GAS_ERR_INVALID, "count_active: null argument");
   if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (c->densePending) {
+    gas_status st = set_device(c);
+    if (!st) st = materialize(c);
+    if (st) return st;
+  }
   if (c->rangeMode) {
     *n = c->rcount;
     return GAS_OK;
@@ -726,6 +791,8 @@ gas_status gas_core_gather_apply(gas_core *c, int32_t haveGather, gas_gather_lau
   if (!c || !launch) return fail(GAS_ERR_INVALID, "gather_apply: null argument");
   if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
   gas_status st = set_device(c);
+  if (st) return st;
+  st = materialize(c);
   if (st) return st;
   st = clean(c, sbit(c->sidx) | kT0);
   if (st) return st;
@@ -829,6 +896,11 @@ gas_status gas_core_scatter_activate(gas_core *c) {
 gas_status gas_core_next_iter(gas_core *c) {
   if (!c) return fail(GAS_ERR_INVALID, "next_iter: engine is NULL");
   if (!c->haveGraph) return fail(GAS_ERR_STATE, "no graph set");
+  if (c->densePending) {
+    gas_status st = set_device(c);
+    if (!st) st = materialize(c);
+    if (st) return st;
+  }
   c->cur ^= 1;
   c->sidx ^= 1;
   c->rangeMode = false;
@@ -1021,6 +1093,7 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
       (c->rangeMode && c->rstart == 0 && c->rcount == c->nV && ra.denseAlpha > 0) ? 1 : 0;
   ra.vcurOut = &c->ctl->vcur;
   ra.resume = &c->ctl->resume[0];
+  ra.denseEndOut = &c->ctl->denseEnd;
 
   cudaEventRecord(c->t0, c->stream);
   st = runLaunch(user, &ra, (void *)c->stream);
@@ -1031,7 +1104,7 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "persistent run launch");
   cudaEventRecord(c->t1, c->stream);
-  int32_t rv[2] = {0, 0};  // rounds, vcur (adjacent in Ctl)
+  int32_t rv[4] = {0, 0, 0, 0};  // rounds, vcur, denseEnd, pad (adjacent in Ctl)
   A(cudaMemcpyAsync(rv, &c->ctl->rounds, sizeof(rv), cudaMemcpyDeviceToHost, c->stream));
   A(cudaStreamSynchronize(c->stream));
   if (e != cudaSuccess) return cuda_fail(e, "persistent run");
@@ -1057,6 +1130,11 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   c->pendingCommit = false;
   c->haveScatList = false;
   c->countValid = false;
+  if (rv[2] && R > 0) {  // the next frontier is the last round's stamps
+    c->densePending = true;
+    c->densePendStamp = c->stamp;  // the last round's stamp
+    c->densePendArr = (R - 1) & 1;
+  }
   if (iterations) *iterations = R;
   return check_device_error(c);
 }
