@@ -817,7 +817,7 @@ def run_serve_c5(args):
     gas.load()
     stream = torch.cuda.current_stream()
     gs = c5_graphs(set(args.c5_graphs.split(",")) if args.c5_graphs else None)
-    srv = gas.GASServer(device=local, lanes=C5_LANES)
+    srv = gas.GASServer(device=local, lanes=args.c5_lanes)
     ids = [srv.add_graph(g.n_vertices, g.srcs, g.dsts, g.weights) for _, g in gs]
     bufs = [(torch.empty(g.n_vertices, dtype=torch.int32).pin_memory().numpy(),
              torch.empty(g.n_vertices, dtype=torch.float32).pin_memory().numpy()) for _, g in gs]
@@ -883,7 +883,7 @@ def run_serve_c5(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * span / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
         "config": {"workload": "serve-c5", "desc": WORKLOADS["serve-c5"]["desc"], "seed": SEED,
-                   "queries_per_step": C5_QUERIES, "lanes": C5_LANES, "max_batch": 256,
+                   "queries_per_step": C5_QUERIES, "lanes": args.c5_lanes, "max_batch": 256,
                    "graphs": {n: [g.n_vertices, g.n_edges] for n, g in gs},
                    "arrivals": "timed steps: every query of the step offered at once (capacity); "
                                "sweep: Poisson at fractions of that capacity",
@@ -929,6 +929,8 @@ def main():
                     help="batch-c4: default launch configuration instead of the autotuner")
     ap.add_argument("--c4-delta", type=int, default=0,
                     help="batch-c4 with --no-autotune: SSSP bucket width")
+    ap.add_argument("--c5-lanes", type=int, default=C5_LANES,
+                    help="serve-c5: batches in flight at once")
     ap.add_argument("--c5-graphs", default=None,
                     help="serve-c5: comma-separated subset of the graphs, e.g. rmat20 (profiling)")
     args = ap.parse_args()
