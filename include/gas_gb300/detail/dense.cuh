@@ -9,17 +9,19 @@
 //   vertex v is active in round r+1  <=>  some in-neighbour u of v returned
 //   true in round r  (retStamp[r & 1][u] == stamp of round r)
 //
-// The stamps of consecutive rounds live in two arrays, so a round reads the
-// previous round's set while it records its own.
-//
 // which is exactly the set the reference's scatterActivate builds, so the
-// active sets and round counts are unchanged.  The pass gathers
-// speculatively, applies to the active vertices and writes every vertex's
-// data to the other buffer of a ping-pong pair: no commit, no scatter
-// traversal, no frontier list, one grid barrier per round.
+// active sets and round counts are unchanged.  The stamps of consecutive
+// rounds live in two arrays, so a round reads the previous round's set
+// while it records its own.  The pass gathers speculatively, applies to the
+// active vertices and writes every vertex's data to the other buffer of a
+// ping-pong pair: no commit, no scatter traversal, no frontier list, one
+// grid barrier per round.  A list round with a large frontier can run the
+// same pass in mark mode: the active vertices are those the previous
+// scatter marked, and the others gather nothing.
 //
-// Load balance is fixed per graph by in-degree bins, each vertex owned by
-// one warp work unit, with no block barriers and no waits:
+// Work units follow in-degree bins fixed per graph, each vertex owned by
+// one warp work unit, with no block barriers and no waits; warps take the
+// units heaviest first (dense_pass):
 //   in-degree 0..8      one thread, edges folded left to right from
 //                       gatherZero (the order of refgas.h:147-158);
 //   in-degree 9..64     8 lanes, ordered shuffle tree;
