@@ -323,15 +323,20 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
   }
 }
 
-// Flushes a warp's counts (one pair of atomics per warp and pass).
+// Flushes the block's counts: one pair of atomics per block and pass (the
+// caller's grid barrier follows).
 __device__ __forceinline__ void dense_flush(const DenseCtx &a, const DenseCounts &c) {
+  __shared__ unsigned long long sA[32], sR[32];
   const unsigned wA = __reduce_add_sync(kFullMask, c.active);
   const unsigned wEin = __reduce_add_sync(kFullMask, c.inEdges);
   const unsigned wR = __reduce_add_sync(kFullMask, c.ret);
   const unsigned wEout = __reduce_add_sync(kFullMask, c.outEdges);
-  if ((threadIdx.x & 31) == 0) {
-    if (wA) atomicAdd(a.cnt, ((unsigned long long)wA << 32) | wEin);
-    if (wR) atomicAdd(a.cnt + 1, ((unsigned long long)wR << 32) | wEout);
+  if ((threadIdx.x & 31) == 0) sR[threadIdx.x >> 5] = ((unsigned long long)wR << 32) | wEout;
+  block_add_u64(((unsigned long long)wA << 32) | wEin, a.cnt, sA);
+  if (threadIdx.x == 0) {
+    unsigned long long s = 0ull;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sR[k];
+    if (s) atomicAdd(a.cnt + 1, s);
   }
 }
 

@@ -127,8 +127,8 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
   }
 #pragma unroll
   for (int k = 0; k < D; ++k) dg[k] -= bg[k];
-  if (warpAppend)  // the next round's consumer is one thread per entry: no split hints
-    warp_append_list<D>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
+  if (warpAppend)  // the next round is fused again: one thread per entry, degrees <= 8
+    warp_append_list<D, false>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
   else
     block_append<kSNT, D, GAS_GATHER_TILE>(ok, dst, dg, bg, sa.next, sa.maxGatherTiles, a.capacity,
                                            a.errWord, sm.app);

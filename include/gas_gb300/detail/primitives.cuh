@@ -349,11 +349,28 @@ __device__ __forceinline__ void block_append(const bool (&ok)[K], const int32_t 
   __syncthreads();
 }
 
+// Adds a per-warp 64-bit value (lane 0's v) into *target with one atomic per
+// block (per-warp atomics on one address serialise at its L2 slice).  Every
+// thread of the block calls it; sm holds one word per warp and is free again
+// after the block's next barrier.
+__device__ __forceinline__ void block_add_u64(unsigned long long v, unsigned long long *target,
+                                              unsigned long long *sm) {
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long s = 0ull;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += sm[k];
+    if (s) atomicAdd(target, s);
+  }
+}
+
 // warp_append: block_append for one warp, without split hints (for lists
 // whose consumer walks one thread per entry): the warp reserves its
 // (count, degree sum) with one atomicAdd on the packed counter and every
 // lane writes its own entries.  No shared memory, no block barrier.
-template <int K>
+// kMaxDeg false leaves the list's maximum degree alone (a consumer that
+// knows every degree is small does not read it).
+template <int K, bool kMaxDeg = true>
 __device__ __forceinline__ void warp_append_list(const bool (&ok)[K], const int32_t (&vid)[K],
                                                  const int32_t (&deg)[K], const int32_t (&beg)[K],
                                                  const gas_vertex_list &out, int32_t capacity,
@@ -380,7 +397,7 @@ __device__ __forceinline__ void warp_append_list(const bool (&ok)[K], const int3
   unsigned long long base = 0ull;
   if (lane == 0) {
     base = atomicAdd(out.count, total);
-    atomicMax(out.maxDeg, wmax);
+    if (kMaxDeg) atomicMax(out.maxDeg, wmax);
   }
   base = __shfl_sync(kFullMask, base, 0);
   const unsigned long long excl = incl - mine;
