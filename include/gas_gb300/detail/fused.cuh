@@ -45,17 +45,17 @@ __device__ __forceinline__ VD fused_read(const FusedCtx &f, int v) {
 // warp, no block barrier); larger ones per block (one atomic per block).
 constexpr int kWarpAppendMax = 4096;
 
-// One tile of GAS_TPV_TILE frontier vertices.  Counts this round's
+// Frontier entry i (none when i >= n) for this thread.  Counts this round's
 // apply-returned-true vertices and their out-edges into cRet / cOut.
 // warpAppend (block-uniform): append the activated vertices per warp.
+// Every thread of the block calls it (the appends are collective).
 template <class P>
 __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const ScatterArgs &sa, const FusedCtx &f,
-                               int t, int n, int T, bool warpAppend, ScatterSmem &sm, unsigned &cRet,
+                               int i, int n, int T, bool warpAppend, ScatterSmem &sm, unsigned &cRet,
                                unsigned &cOut) {
   typedef typename P::VertexData VD;
   typedef typename P::GatherResult GR;
   constexpr int D = GAS_TPV_MAX_DEGREE;
-  const int i = t * GAS_TPV_TILE + threadIdx.x;
   bool isEdge[D];
   int32_t dst[D];
 #pragma unroll

@@ -321,10 +321,13 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         sa.next = ra.frontL[cur ^ 1];
         sa.stamp = stamp;
         unsigned cRet = 0u, cOut = 0u;
-        const int ntF = (n + GAS_TPV_TILE - 1) / GAS_TPV_TILE;
         const bool warpAppend = n <= kWarpAppendMax;
-        for (int t = blockIdx.x; t < ntF; t += gridDim.x) {
-          fused_tpv_tile<P>(a, sa, f, t, n, T, warpAppend, sm.s, cRet, cOut);
+        // entries dealt across all blocks (entry base + k*grid + block), so a
+        // frontier of a few tiles still spreads its loads over every SM
+        const int per = gridDim.x * blockDim.x;
+        for (int base = 0; base < n; base += per) {
+          fused_tpv_tile<P>(a, sa, f, base + (int)threadIdx.x * (int)gridDim.x + (int)blockIdx.x, n, T,
+                            warpAppend, sm.s, cRet, cOut);
           if (!warpAppend) __syncthreads();
         }
         cRet = __reduce_add_sync(kFullMask, cRet);
