@@ -480,6 +480,9 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
   __shared__ unsigned sNear[W];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
   const long long gw = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  // list entries are dealt to warps block-first (warp k of every block, then
+  // warp k+1), so a short list spreads over every SM
+  const long long gwl = (long long)(threadIdx.x / 32) * gridDim.x + blockIdx.x;
   const size_t maskWords = (size_t)a.nVertices * W;
   const bool buckets = KIND == kBatchSSSP && a.delta > 0;
   const BatchBucket bk{buckets ? sBound : nullptr, buckets ? sNear : nullptr};
@@ -528,14 +531,14 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       const uint32_t *pc = a.pairs[rc];
       uint32_t *pn = a.pairs[rn];
       const long long threads = (long long)gridDim.x * blockDim.x;
-      for (long long base = gw * 32; base < nList; base += threads) {
+      for (long long base = gwl * 32; base < nList; base += threads) {
         const long long i = base + (threadIdx.x & 31);
         const bool valid = i < nList;
         batch_pair_unit<W, KIND>(a, valid, valid ? __ldcg(pc + i) : 0u, r, cur, nxt,
                                  pn, cntNext, changed, bk);
       }
     } else if (push) {
-      for (long long i = gw; i < nList; i += warps)
+      for (long long i = gwl; i < nList; i += warps)
         batch_push_unit<W, KIND>(a, listCur[i], listCurC[i], r, cur, nxt, listNext, listNextC,
                                  cntNext, changed, bk);
     } else {
