@@ -4,16 +4,17 @@
 // barrier instead of two (gather -> barrier -> commit + scatter ->
 // barrier).
 //
-// Bulk-synchronous reads without a commit step: vertex data has two slots
-// per vertex (the engine's two buffers) and a version word per vertex,
-//   ver[v] = (round stamp << 1) | slot holding v's newest value.
-// A vertex applied in round S writes the slot it is not in and publishes
-// (S, that slot).  Every read in round S wants the value as of the end of
-// round S-1: when v's word already says S, that is the other slot (which
-// the writer never touches in round S), otherwise the slot in the word --
-// so readers need no ordering against the writer.  Active sets, round
-// counts and results are those of the two-phase rounds; versioned data is
-// folded back into the first slot before a dense round and at the end of
+// Bulk-synchronous reads without a commit step: for the fused rounds of a
+// run, vertex data moves into cells, one per vertex,
+//   { value slot 0, value slot 1, ver = (round stamp << 1) | newest slot },
+// 16-byte aligned so that one vector load reads a whole cell.  A vertex
+// applied in round S writes the slot it is not in and publishes (S, that
+// slot).  Every read in round S wants the value as of the end of round S-1:
+// when v's word already says S, that is the other slot (which the writer
+// never touches in round S), otherwise the slot in the word -- so readers
+// need no ordering against the writer.  Active sets, round counts and
+// results are those of the two-phase rounds; the newest values go back to
+// the vertex data array before a dense or two-phase round and at the end of
 // the run.
 #pragma once
 
@@ -23,22 +24,56 @@
 namespace gas {
 namespace detail {
 
+template <class VD>
+struct alignas(16) FusedCell {
+  VD s[2];
+  uint32_t ver;
+};
+
+
 struct FusedCtx {
-  void *slot[2];        // vertex data: slot 0 = the run's current buffer
-  uint32_t *ver;        // [V] (stamp << 1) | slot
+  void *cells;          // [V] FusedCell<VD> (Programs with a gather)
+  void *vd;             // the run's vertex data (apply-only Programs update it in place)
   uint32_t stamp;       // this round's stamp
   int32_t *retStamp;    // [V] stamp of the round whose apply returned true
 };
 
-// v's value as of the end of the previous round.  The word and both slots
-// are loaded together (one round trip), then the right slot is kept.
+// One cell, read from L2 (written by other CTAs) with 16-byte loads.
+template <class VD>
+__device__ __forceinline__ FusedCell<VD> load_cell(const FusedCell<VD> *p) {
+  static_assert(sizeof(FusedCell<VD>) % 16 == 0, "cells are whole 16-byte words");
+  constexpr int N = (int)(sizeof(FusedCell<VD>) / 16);
+  union {
+    int4 w[N];
+    FusedCell<VD> c;
+  } u;
+#pragma unroll
+  for (int k = 0; k < N; ++k) u.w[k] = __ldcg(reinterpret_cast<const int4 *>(p) + k);
+  return u.c;
+}
+
+// v's value as of the end of the previous round.
 template <class VD>
 __device__ __forceinline__ VD fused_read(const FusedCtx &f, int v) {
-  const uint32_t w = __ldcg(f.ver + v);
-  const VD x0 = load_cg(reinterpret_cast<const VD *>(f.slot[0]) + v);
-  const VD x1 = load_cg(reinterpret_cast<const VD *>(f.slot[1]) + v);
-  const uint32_t s = ((w >> 1) == f.stamp) ? (1u - (w & 1u)) : (w & 1u);
-  return s ? x1 : x0;
+  const FusedCell<VD> c = load_cell(reinterpret_cast<const FusedCell<VD> *>(f.cells) + v);
+  const uint32_t s = ((c.ver >> 1) == f.stamp) ? (1u - (c.ver & 1u)) : (c.ver & 1u);
+  return s ? c.s[1] : c.s[0];
+}
+
+// Every vertex's value into slot 0 of its cell, version 0 (before the first
+// fused round of a run; a grid barrier follows).
+template <class P>
+__device__ void fused_enter(const FusedCtx &f, const void *vd, int nVertices) {
+  typedef typename P::VertexData VD;
+  // the library allocates GAS_FUSED_CELL_BYTES(sizeof(VertexData)) per vertex
+  static_assert(sizeof(FusedCell<VD>) == GAS_FUSED_CELL_BYTES(sizeof(VD)),
+                "VertexData alignment above 16 bytes");
+  FusedCell<VD> *cells = reinterpret_cast<FusedCell<VD> *>(f.cells);
+  const int stride = gridDim.x * blockDim.x;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nVertices; v += stride) {
+    cells[v].s[0] = reinterpret_cast<const VD *>(vd)[v];
+    cells[v].ver = 0u;
+  }
 }
 
 // Frontiers of at most this many vertices append per warp (one atomic per
@@ -68,11 +103,16 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
     front_entry(a, i, n, T, v, pre, end, beg);
     const int deg = end - pre;
     const int obeg = a.outOffsets[v], oend = a.outOffsets[v + 1];
-    const uint32_t wv = __ldcg(f.ver + v);
-    const VD own0 = load_cg(reinterpret_cast<const VD *>(f.slot[0]) + v);
-    const VD own1 = load_cg(reinterpret_cast<const VD *>(f.slot[1]) + v);
-    const int own = (int)(wv & 1u);  // v is applied once per round: its word is still old
-    VD tmp = own ? own1 : own0;
+    FusedCell<VD> *cell = reinterpret_cast<FusedCell<VD> *>(f.cells) + v;
+    int own = 0;
+    VD tmp;
+    if (a.haveGather) {
+      const FusedCell<VD> c = load_cell(cell);
+      own = (int)(c.ver & 1u);  // v is applied once per round: its word is still old
+      tmp = own ? c.s[1] : c.s[0];
+    } else {
+      tmp = reinterpret_cast<const VD *>(f.vd)[v];
+    }
     // out-neighbours loaded before apply decides whether they are activated
     const int odeg = oend - obeg;
     int32_t outd[D];
@@ -93,12 +133,12 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
         if (k < deg)
           acc = P::gatherReduce(acc, P::gatherMap(&tmp, &sv[k], edge_ptr<P>(a.edgeData, beg + k)));
       r = do_apply<P>(&tmp, acc, a.iteration);
-      reinterpret_cast<VD *>(f.slot[own ^ 1])[v] = tmp;
-      f.ver[v] = (f.stamp << 1) | (uint32_t)(own ^ 1);
+      cell->s[own ^ 1] = tmp;
+      cell->ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
     } else {  // apply only: nothing reads other vertices, update in place
       const GR gz = P::gatherZero;
       r = do_apply<P>(&tmp, gz, a.iteration);
-      reinterpret_cast<VD *>(f.slot[own])[v] = tmp;
+      reinterpret_cast<VD *>(f.vd)[v] = tmp;
     }
     if (r) {
       f.retStamp[v] = (int32_t)f.stamp;
@@ -134,17 +174,15 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
                                            a.errWord, sm.app);
 }
 
-// Every vertex's newest value into slot 0 (the run's current buffer).
+// Every vertex's newest value back into the run's vertex data (f.vd).
 template <class P>
 __device__ void fused_fold(const FusedCtx &f, int nVertices) {
   typedef typename P::VertexData VD;
+  const FusedCell<VD> *cells = reinterpret_cast<const FusedCell<VD> *>(f.cells);
   const int stride = gridDim.x * blockDim.x;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nVertices; v += stride) {
-    const uint32_t w = __ldcg(f.ver + v);
-    if (w & 1u) {
-      reinterpret_cast<VD *>(f.slot[0])[v] = load_cg(reinterpret_cast<const VD *>(f.slot[1]) + v);
-      f.ver[v] = w & ~1u;
-    }
+    const FusedCell<VD> c = load_cell(cells + v);
+    reinterpret_cast<VD *>(f.vd)[v] = (c.ver & 1u) ? c.s[1] : c.s[0];
   }
 }
 

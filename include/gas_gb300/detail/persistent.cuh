@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   const long long E = a.nEdges;
 
   int cur = ra.cur, sidx = ra.sidx, vcur = 0;
-  bool versioned = false;  // some vertex's newest value sits in the second buffer
+  bool versioned = false;  // the vertex data lives in the fused cells
   bool rangeMode = a.rangeMode != 0;
   int mode = ra.allActive ? kDense : kList;
   bool allActive = ra.allActive != 0;
@@ -313,11 +313,15 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       if (ra.fused && (tpvG || !a.haveGather)) {
         // ---------------- fused round: one phase, one barrier
         FusedCtx f;
-        f.slot[0] = vdBuf[vcur];
-        f.slot[1] = vdBuf[vcur ^ 1];
-        f.ver = ra.ver;
+        f.cells = ra.fusedCells;
+        f.vd = vdBuf[vcur];
         f.stamp = (uint32_t)stamp;
         f.retStamp = ra.retStamp[r & 1];
+        if (a.haveGather && !versioned) {  // the vertex data moves into the cells
+          fused_enter<P>(f, vdBuf[vcur], a.nVertices);
+          versioned = true;
+          if (!grid_barrier(ra.barrier, a.errWord)) break;
+        }
         sa.next = ra.frontL[cur ^ 1];
         sa.stamp = stamp;
         unsigned cRet = 0u, cOut = 0u;
@@ -334,24 +338,22 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         cOut = __reduce_add_sync(kFullMask, cOut);
         unsigned long long *rc = ra.denseCnt + kDenseCntStride * (r % 3) + 1;
         if ((threadIdx.x & 31) == 0 && cRet) atomicAdd(rc, ((unsigned long long)cRet << 32) | cOut);
-        versioned = versioned || a.haveGather;
         if (!grid_barrier(ra.barrier, a.errWord)) break;
         statA = ((unsigned long long)n << 32) | (unsigned)T;
         statR = *rc;
         const int nr = (int)(statR >> 32);
         denseNext = ra.denseAlpha > 0 && nr > 0 &&
                     (long long)(statR & 0xffffffffull) * ra.denseAlpha > E;
-        if (denseNext && versioned) {  // dense rounds read the first buffer whole
+        if (denseNext && versioned) {  // dense rounds read the vertex data array
           fused_fold<P>(f, a.nVertices);
           versioned = false;
           if (!grid_barrier(ra.barrier, a.errWord)) break;
         }
       } else {
-      if (versioned) {  // two-phase rounds read the first buffer
+      if (versioned) {  // two-phase rounds read the vertex data array
         FusedCtx f;
-        f.slot[0] = vdBuf[vcur];
-        f.slot[1] = vdBuf[vcur ^ 1];
-        f.ver = ra.ver;
+        f.cells = ra.fusedCells;
+        f.vd = vdBuf[vcur];
         fused_fold<P>(f, a.nVertices);
         versioned = false;
         if (!grid_barrier(ra.barrier, a.errWord)) break;
@@ -430,9 +432,8 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   }
   if (versioned) {  // the newest values into the run's current buffer
     FusedCtx f;
-    f.slot[0] = vdBuf[vcur];
-    f.slot[1] = vdBuf[vcur ^ 1];
-    f.ver = ra.ver;
+    f.cells = ra.fusedCells;
+    f.vd = vdBuf[vcur];
     fused_fold<P>(f, a.nVertices);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -41,6 +41,10 @@ extern "C" {
 #define GAS_TPV_MAX_DEGREE 8
 #define GAS_TPV_TILE GAS_GATHER_THREADS
 
+/* Bytes of one vertex's cell in fused rounds: two value slots and a version
+ * word, rounded up to 16 (one aligned vector load reads a whole cell). */
+#define GAS_FUSED_CELL_BYTES(vertexBytes) ((((vertexBytes) * 2 + 4) + 15) / 16 * 16)
+
 /* A vertex list on the device: ids, exclusive prefix of the degree that the
  * consumer walks (in-degree for the gather, out-degree for the scatter),
  * CSC/CSR begin offset of each vertex, merge-path tile splits, and a
@@ -149,7 +153,8 @@ typedef struct {
   /* fused list rounds (every degree <= 8): gather, apply and activation in
    * one phase, vertex data versioned across the two buffers */
   int32_t fused;
-  uint32_t *ver;              /* [V] (stamp << 1) | buffer of the newest value */
+  void *fusedCells;           /* [V] cells of GAS_FUSED_CELL_BYTES(vertexBytes) each:
+                                 two value slots and (stamp << 1) | newest slot */
   /* the run starts with dense rounds (allActive): the caller may run them in
    * a leaner kernel first, which leaves the state the main kernel resumes
    * from in resume[4] = rounds done, vcur, dense -> list transition pending,

@@ -130,7 +130,7 @@ struct gas_core_s {
   uint32_t *csrPerm = nullptr;  // [E] the same for the CSR, kept on request
   bool keepCsrPerm = false;
   int32_t *csr2csc = nullptr;   // [E] CSC position of each CSR edge (Program::scatter)
-  uint32_t *ver = nullptr;      // [V] version words of fused rounds (fused.cuh)
+  void *fcell = nullptr;        // [V] cells of fused rounds (fused.cuh), fused-eligible graphs only
   int32_t maxOutDeg = 0;
   bool fusedRounds = true;      // one-phase rounds when every degree is <= 8
   bool edgeScatterOn = false;   // keep csr2csc and run scatter-capable rounds
@@ -204,12 +204,12 @@ void free_graph(gas_core *c) {
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
                   c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats,
-                  c->cscPerm, c->csrPerm, c->csr2csc, c->ver};
+                  c->cscPerm, c->csrPerm, c->csr2csc, c->fcell};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->cscPerm = c->csrPerm = nullptr;
   c->csr2csc = nullptr;
-  c->ver = nullptr;
+  c->fcell = nullptr;
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
   c->retStamp[0] = c->retStamp[1] = nullptr;
@@ -558,13 +558,14 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(cudaMalloc(&c->valt, (size_t)vertexBytes * std::max(nV, 1)));
   A(dalloc(&c->retStamp[0], (size_t)nV));
   A(dalloc(&c->retStamp[1], (size_t)nV));
-  A(dalloc(&c->ver, (size_t)nV));
   c->maxInDeg = 0;
   c->maxOutDeg = 0;
   for (int32_t v = 0; v < nV; ++v) {
     c->maxInDeg = std::max(c->maxInDeg, c->hInOff[(size_t)v + 1] - c->hInOff[v]);
     c->maxOutDeg = std::max(c->maxOutDeg, c->hOutOff[(size_t)v + 1] - c->hOutOff[v]);
   }
+  if (c->maxInDeg <= GAS_TPV_MAX_DEGREE && c->maxOutDeg <= GAS_TPV_MAX_DEGREE)  // fused rounds
+    A(cudaMalloc(&c->fcell, (size_t)GAS_FUSED_CELL_BYTES(vertexBytes) * std::max(nV, 1)));
   // in-degree bins of the dense pass
   std::vector<int32_t> bMid, bSmall, bTiny, chV, chB, chF, chC, chS;
   for (int32_t v = 0; v < nV; ++v) {
@@ -631,7 +632,6 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
     return cuda_fail(e, "setGraph device allocation");
   }
   A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
-  A(cudaMemsetAsync(c->ver, 0, sizeof(uint32_t) * std::max(nV, 1), c->stream));
   for (int k = 0; k < 2; ++k)
     A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
   auto up = [&](int32_t *dst, const std::vector<int32_t> &src) {
@@ -1010,7 +1010,6 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
     A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
     for (int k = 0; k < 2; ++k)
       A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
-    A(cudaMemsetAsync(c->ver, 0, sizeof(uint32_t) * std::max(c->nV, 1), c->stream));
     c->stamp = 0;
   }
   A(cudaMemsetAsync(&c->ctl->dense[0][0], 0, sizeof(c->ctl->dense), c->stream));
@@ -1081,8 +1080,8 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.chunkVal = c->chunkVal;
   ra.chunkFlags = c->chunkFlags;
   ra.denseCnt = &c->ctl->dense[0][0];
-  ra.ver = c->ver;
-  ra.fused = (c->fusedRounds && !c->csr2csc && c->maxInDeg <= GAS_TPV_MAX_DEGREE &&
+  ra.fusedCells = c->fcell;
+  ra.fused = (c->fcell && c->fusedRounds && !c->csr2csc && c->maxInDeg <= GAS_TPV_MAX_DEGREE &&
               c->maxOutDeg <= GAS_TPV_MAX_DEGREE)
                  ? 1
                  : 0;
