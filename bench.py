@@ -61,12 +61,12 @@ RMAT_SCALE = {"pagerank-rmat22": 22, "cc-rmat22": 22}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per run (the
 # run's kernels) from ncu captures of the same command (profiles/): the
 # lattice run's main kernel directly (its one-round dense kernel is 0.15 %
-# of the time and not counted); PageRank's two kernels on R-MAT-20 (4.088
+# of the time and not counted); PageRank's two kernels on R-MAT-20 (3.943
 # GB per run, 16.09 M edges) scaled by edges, its traffic being per-edge
 # gathers and the CSC stream.  None where no capture exists.
 TRAFFIC_PER_LAUNCH = {
-    "sssp-grid1024": 74.617344e6 + 9.072896e6,
-    "pagerank-rmat22": (2.860072e9 + 0.458806e9 + 0.668338e9 + 0.100529e9) * (65244320 / 16086703),
+    "sssp-grid1024": 84.358144e6 + 17.835520e6,
+    "pagerank-rmat22": (2.757832e9 + 0.411875e9 + 0.672337e9 + 0.101243e9) * (65244320 / 16086703),
 }
 
 
