@@ -77,7 +77,8 @@ __device__ void fused_enter(const FusedCtx &f, const void *vd, int nVertices) {
 }
 
 // Frontiers of at most this many vertices append per warp (one atomic per
-// warp, no block barrier); larger ones per block (one atomic per block).
+// warp, no block barrier); larger ones per block (one atomic per block, two
+// block barriers).
 constexpr int kWarpAppendMax = 4096;
 
 // Frontier entry i (none when i >= n) for this thread.  Counts this round's
@@ -86,8 +87,7 @@ constexpr int kWarpAppendMax = 4096;
 // Every thread of the block calls it (the appends are collective).
 template <class P>
 __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const ScatterArgs &sa, const FusedCtx &f,
-                               int i, int n, int T, bool warpAppend, ScatterSmem &sm, unsigned &cRet,
-                               unsigned &cOut) {
+                               int i, int n, int T, bool warpAppend, unsigned &cRet, unsigned &cOut) {
   typedef typename P::VertexData VD;
   typedef typename P::GatherResult GR;
   constexpr int D = GAS_TPV_MAX_DEGREE;
@@ -167,11 +167,12 @@ __device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const S
   }
 #pragma unroll
   for (int k = 0; k < D; ++k) dg[k] -= bg[k];
-  if (warpAppend)  // the next round is fused again: one thread per entry, degrees <= 8
+  // the next round is fused again: one thread per entry, every degree <= 8
+  // (no split hints, no maximum degree)
+  if (warpAppend)
     warp_append_list<D, false>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
   else
-    block_append<kSNT, D, GAS_GATHER_TILE>(ok, dst, dg, bg, sa.next, sa.maxGatherTiles, a.capacity,
-                                           a.errWord, sm.app);
+    block_append_list<D, false>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
 }
 
 // Every vertex's newest value back into the run's vertex data (f.vd).

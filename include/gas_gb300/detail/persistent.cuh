@@ -331,8 +331,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         const int per = gridDim.x * blockDim.x;
         for (int base = 0; base < n; base += per) {
           fused_tpv_tile<P>(a, sa, f, base + (int)threadIdx.x * (int)gridDim.x + (int)blockIdx.x, n, T,
-                            warpAppend, sm.s, cRet, cOut);
-          if (!warpAppend) __syncthreads();
+                            warpAppend, cRet, cOut);
         }
         cRet = __reduce_add_sync(kFullMask, cRet);
         cOut = __reduce_add_sync(kFullMask, cOut);

@@ -418,5 +418,73 @@ __device__ __forceinline__ void warp_append_list(const bool (&ok)[K], const int3
     }
 }
 
+// block_append_list: warp_append_list with one atomic per block instead of
+// one per warp (a large frontier's appends would otherwise serialise on the
+// list counter): the warps' totals meet in shared memory, thread 0 reserves
+// the block's range, and every lane writes its own entries.  No split
+// hints, no staging of the entries.  Every thread of the block calls it.
+template <int K, bool kMaxDeg = true>
+__device__ __forceinline__ void block_append_list(const bool (&ok)[K], const int32_t (&vid)[K],
+                                                  const int32_t (&deg)[K], const int32_t (&beg)[K],
+                                                  const gas_vertex_list &out, int32_t capacity,
+                                                  unsigned *errWord) {
+  __shared__ unsigned long long sTot[32];
+  __shared__ unsigned long long sBase[32];
+  __shared__ unsigned sMax;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned cnt = 0, esum = 0, dmax = 0;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (ok[k]) {
+      ++cnt;
+      esum += (unsigned)deg[k];
+      dmax = max(dmax, (unsigned)deg[k]);
+    }
+  const unsigned long long mine = ((unsigned long long)cnt << 32) | esum;
+  unsigned long long incl = mine;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned long long o = __shfl_up_sync(kFullMask, incl, d);
+    if (lane >= d) incl += o;
+  }
+  const unsigned wmax = kMaxDeg ? __reduce_max_sync(kFullMask, dmax) : 0u;
+  if (lane == 31) sTot[warp] = incl;
+  if (kMaxDeg && threadIdx.x == 0) sMax = 0u;
+  __syncthreads();
+  if (kMaxDeg && lane == 0 && wmax) atomicMax(&sMax, wmax);
+  if (threadIdx.x == 0) {
+    unsigned long long run = 0ull;
+    for (int w = 0; w < nw; ++w) {
+      const unsigned long long t = sTot[w];
+      sTot[w] = run;  // exclusive prefix of the warps' totals
+      run += t;
+    }
+    unsigned long long base = 0ull;
+    if (run) base = atomicAdd(out.count, run);
+    sBase[0] = base;
+    sBase[1] = run;
+  }
+  __syncthreads();
+  const unsigned long long base = sBase[0], total = sBase[1];
+  if (total == 0ull) return;  // block-uniform
+  if (kMaxDeg && threadIdx.x == 0 && sMax) atomicMax(out.maxDeg, sMax);
+  if ((long long)(base >> 32) + (long long)(total >> 32) > capacity) {
+    if (threadIdx.x == 0) atomicOr(errWord, GAS_DEVERR_CAPACITY);
+    return;
+  }
+  const unsigned long long off = sTot[warp] + (incl - mine);
+  long long q = (long long)(base >> 32) + (long long)(off >> 32);
+  long long e = (long long)(base & 0xffffffffull) + (long long)(off & 0xffffffffull);
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (ok[k]) {
+      out.vid[q] = vid[k];
+      out.pre[q] = (int32_t)e;
+      out.beg[q] = beg[k];
+      ++q;
+      e += deg[k];
+    }
+}
+
 }  // namespace detail
 }  // namespace gas
