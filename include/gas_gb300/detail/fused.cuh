@@ -79,7 +79,7 @@ __device__ void fused_enter(const FusedCtx &f, const void *vd, int nVertices) {
 // Frontiers of at most this many vertices append per warp (one atomic per
 // warp, no block barrier); larger ones per block (one atomic per block, two
 // block barriers).
-constexpr int kWarpAppendMax = 4096;
+constexpr int kWarpAppendMax = 16384;
 
 // Frontier entry i (none when i >= n) for this thread.  Counts this round's
 // apply-returned-true vertices and their out-edges into cRet / cOut.
