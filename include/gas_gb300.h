@@ -111,7 +111,9 @@ GAS_API gas_status gas_engine_next_iter(gas_engine *e, int32_t *nActive);
 
 /* Replaces run (gpugas.h:764-772): iterate until no vertex is active, or
  * for at most maxIters rounds when maxIters > 0.  iterations (may be NULL)
- * receives the number of non-empty rounds executed. */
+ * receives the number of non-empty rounds executed.  After a run that
+ * stopped at maxIters, a later run or the stepwise calls continue from the
+ * next round's frontier. */
 GAS_API gas_status gas_engine_run(gas_engine *e, int32_t maxIters, int32_t *iterations);
 
 /* Replaces the BFS driver's setIterationCount<true> (bfs.cu:81-88,
