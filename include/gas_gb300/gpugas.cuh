@@ -163,11 +163,13 @@ class EngineGPU {
   void setPersistent(bool on) { persistent_ = on; }
 
   // CTAs per SM of the persistent run kernel (0 = the default: 2 on graphs
-  // whose degrees are all <= 8, else 4; at most what fits).
+  // whose degrees are all <= 8 -- 1 for apply-only runs --, else 4; at most
+  // what fits).
   void setRunBlocksPerSM(int n) {
     runBlocksPerSM_ = n > 0 ? n : 0;
     runGrid_ = 0;
     runGridFused_ = 0;
+    runGridFusedApply_ = 0;
   }
 
   // Round number handed to apply(v, g, round) by the stepwise API.
@@ -210,6 +212,9 @@ class EngineGPU {
   // dependent gathers are L2-latency bound.
   static constexpr int kFusedBlocksPerSM = 2;
   static constexpr int kRunBlocksPerSM = 4;
+  // Fused rounds of an apply-only run (BFS: no gather, small frontiers) use
+  // 1 CTA per SM of the same kernel: the barrier is cheaper still.
+  static constexpr int kFusedApplyBlocksPerSM = 1;
   // A run that starts with every vertex active runs its leading dense rounds
   // in run_dense_kernel (40 registers, 6 CTAs per SM), then resumes here.
   static constexpr int kDenseBlocksPerSM = 6;
@@ -242,7 +247,8 @@ class EngineGPU {
         self->denseGrid_ = -1;  // not co-resident: the main kernel runs every round
       }
     }
-    int &grid = ra->fused ? self->runGridFused_ : self->runGrid_;
+    const bool applyOnly = ra->fused && !ra->g.haveGather;
+    int &grid = !ra->fused ? self->runGrid_ : (applyOnly ? self->runGridFusedApply_ : self->runGridFused_);
     const void *kern = ra->fused ? (const void *)detail::run_persistent_kernel<Program, kFusedBlocksPerSM>
                                  : (const void *)detail::run_persistent_kernel<Program, kRunBlocksPerSM>;
     if (grid == 0) {
@@ -251,8 +257,9 @@ class EngineGPU {
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, detail::kGNT, 0);
-      const int want = self->runBlocksPerSM_ > 0 ? self->runBlocksPerSM_
-                                                 : (ra->fused ? kFusedBlocksPerSM : kRunBlocksPerSM);
+      const int want = self->runBlocksPerSM_ > 0
+                           ? self->runBlocksPerSM_
+                           : (!ra->fused ? kRunBlocksPerSM : applyOnly ? kFusedApplyBlocksPerSM : kFusedBlocksPerSM);
       if (want > 0 && want < per) per = want;
       grid = (coop && per > 0 && sms > 0) ? per * sms : -1;
     }
@@ -286,6 +293,7 @@ class EngineGPU {
   bool persistent_ = true;
   int runGrid_ = 0;
   int runGridFused_ = 0;
+  int runGridFusedApply_ = 0;
   int denseGrid_ = 0;
   int runBlocksPerSM_ = 0;
   VertexData *vdHost_ = nullptr;
