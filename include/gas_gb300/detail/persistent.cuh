@@ -9,7 +9,9 @@
 //   gather/apply tiles  -> grid barrier -> commit + scatter/activate tiles
 //   -> grid barrier -> swap frontier, next round
 //
-// Rounds whose predecessor activated many out-edges run dense (pull, see
+// On graphs whose degrees are all <= 8 a round is one phase (fused.cuh):
+// a thread per frontier vertex gathers, applies and activates, then one
+// grid barrier.  Rounds whose predecessor activated many out-edges run dense (pull, see
 // dense.cuh): one pass of degree-binned warp units and one barrier.
 // Transitions build the other representation: list -> dense stamps the
 // scatter list, dense -> list compacts the stamped vertices into a scatter
