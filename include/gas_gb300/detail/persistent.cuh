@@ -176,6 +176,10 @@ __device__ __forceinline__ bool dense_to_list(const gas_run_args &ra, const gas_
   return grid_barrier(ra.barrier, a.errWord);
 }
 
+// A list round whose frontier has more than nEdges / kMarkPullFactor in-edges
+// runs as a pull pass over the marked frontier.
+constexpr long long kMarkPullFactor = 4;
+
 // The leading dense rounds of a run that starts with every vertex active,
 // in a kernel that holds nothing else: 40 registers a thread, 6 CTAs per SM
 // (the main kernel's list-round code needs 64 or more).  It stops before
@@ -213,7 +217,16 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_ru
     ++r;
     const int nr = (int)(statR >> 32);
     const long long eout = (long long)(statR & 0xffffffffull);
-    if (!(ra.denseAlpha > 0 && nr > 0 && eout * ra.denseAlpha > E)) {
+    // Dense again when the out-edges of the vertices that returned true are
+    // many (eout * alpha > E, as in the main kernel), and also when they
+    // would activate about V / kMarkPullFactor vertices or more (eout *
+    // kMarkPullFactor > V): a frontier that large has about E /
+    // kMarkPullFactor in-edges at the graph's mean degree, and its list
+    // round would be a pull pass anyway, after a list transition.
+    const bool dense = ra.denseAlpha > 0 && nr > 0 &&
+                       (eout * ra.denseAlpha > E ||
+                        (ra.g.haveGather && eout * kMarkPullFactor > (long long)ra.g.nVertices));
+    if (!dense) {
       pending = nr > 0 ? 1 : 0;  // else the next (list) round is empty
       ended = 1 - pending;
       break;
@@ -226,10 +239,6 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_ru
     ra.resume[3] = ended;
   }
 }
-
-// A list round whose frontier has more than nEdges / kMarkPullFactor in-edges
-// runs as a pull pass over the marked frontier.
-constexpr long long kMarkPullFactor = 4;
 
 // MinBlocks CTAs of 256 threads per SM: the register budget a thread gets
 // (2: 128, 3: 80, 4: 64).
