@@ -1,8 +1,8 @@
 """Benchmark of the GB300 GAS engine (one JSON line on stdout).
 
-Default workload: SSSP on the 1024x1024 4-neighbour lattice with 15% of its
-edges deleted (largest component kept, relabelled row-major), int32 weights
-uniform in [1, 100], source 0, every vertex active at start -- the
+Headline workload: SSSP on the 1024x1024 4-neighbour lattice with 15% of
+its edges deleted (largest component kept, relabelled row-major), int32
+weights uniform in [1, 100], source 0, every vertex active at start -- the
 configuration the reference's GTEPS metric is quoted on for one GPU.
 A step is one full run(): rounds of gather/apply + scatter/activate until no
 vertex is active, from the driver's initial vertex data (sssp.cu:67-82).
@@ -11,13 +11,21 @@ vertex is active, from the driver's initial vertex data (sssp.cu:67-82).
           summed over rounds) / device time, inputs resident in HBM
   e2e     the same through the C ABI with host buffers: vertex data H2D
           from pinned memory, run(), results D2H, every step
-  roofline  the dominant kernel's algorithmic bytes / its CUDA-event time
+  roofline  the run's kernels: algorithmic bytes / their CUDA-event time
   cpu_baseline  the oracle (CPU restatement of the reference engine) on
           the same graph, one run on one core
+  parity  the run's result against the oracle's on the same graph
+
+per_algo (default run on one GPU): the same record for every other
+workload of the metric -- BFS on R-MAT-16, PageRank FP32 and connected
+components on R-MAT-22, the batched queries (256 BFS + 256 SSSP per graph)
+and the serving loop over 8 resident graphs -- each with its own value,
+e2e, roofline or latency figures, CPU baseline and oracle parity.
 
 --impl reference times the reference's CPU engine (oracle/_ref where it
 was built, else the oracle restatement) with every host core running one
-instance of the same workload.
+instance of the headline workload; its graphs come from the oracle's own
+generators, so that process never loads the product library.
 
 Multi-GPU: replicas only (every rank runs the workload on its own GPU; the
 path has no exchange step); value sums the ranks' edges over the slowest
@@ -40,6 +48,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
+SEED = 1
 
 WORKLOADS = {
     "sssp-grid1024": dict(desc="SSSP, 1024x1024 lattice, 15% edges deleted, LCC, w in [1,100], source 0"),
@@ -55,8 +64,10 @@ WORKLOADS = {
                           "rounds) mix on uniform random graph and source; served vs "
                           "one-at-a-time plain engine"),
 }
-SEED = 1
+HEADLINE = "sssp-grid1024"
+PER_ALGO = ("bfs-rmat16", "pagerank-rmat22", "cc-rmat22", "batch-c4", "serve-c5")
 RMAT_SCALE = {"pagerank-rmat22": 22, "cc-rmat22": 22}
+PROGRAM_NAMES = {1: "bfs", 2: "sssp", 3: "cc", 4: "pagerank", 5: "ppr"}
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per run (the
 # run's kernels) from ncu captures of the same command (profiles/): the
@@ -70,28 +81,83 @@ TRAFFIC_PER_LAUNCH = {
 }
 
 
-def make_workload(name: str):
+class Graph:
+    """An edge list (srcs -> dsts, optional int32 weights)."""
+
+    def __init__(self, n_vertices, srcs, dsts, weights=None):
+        self.n_vertices = int(n_vertices)
+        self.srcs, self.dsts, self.weights = srcs, dsts, weights
+
+    @property
+    def n_edges(self) -> int:
+        return int(self.srcs.shape[0])
+
+
+def gen_rmat(scale, seed, symmetrize=False, weights=None, source="product"):
+    """The seeded R-MAT graph: from the product's generator, or ("oracle")
+    from the oracle's independent one (identical edge lists; the reference
+    arm uses it so that its process never loads the product library)."""
+    if source == "oracle":
+        import oracle
+        return Graph(*oracle.port().gen_rmat(scale, 16, seed=seed, symmetrize=symmetrize,
+                                             weights=weights))
     from vertexapi2_gb300 import graphs
-    from vertexapi2_gb300 import programs as P
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_CC, PROGRAM_PAGERANK, PROGRAM_SSSP
+    g = graphs.rmat(scale, 16, seed=seed, symmetrize=symmetrize, weights=weights)
+    return Graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+
+
+def gen_grid(side, seed, weights=(1, 100), source="product"):
+    if source == "oracle":
+        import oracle
+        return Graph(*oracle.port().gen_grid(side, side, 0.15, seed=seed, weights=weights))
+    from vertexapi2_gb300 import graphs
+    g = graphs.grid(side, side, 0.15, seed=seed, weights=weights)
+    return Graph(g.n_vertices, g.srcs, g.dsts, g.weights)
+
+
+def max_outdegree_vertex(n, srcs) -> int:
+    """bfs.cu:148-166: the first vertex with the largest out-degree."""
+    return int(np.argmax(np.bincount(srcs, minlength=n)))
+
+
+def make_workload(name: str, source: str = "product"):
+    """Graph, program and initial state of a plain-engine workload (program
+    ids and initial vertex data as include/gas_gb300.h and the reference
+    drivers define them)."""
+    unreached = 2**31 - 1 - 100000   # sssp.cu:32-33
     if name == "sssp-grid1024":
-        g = graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100))
-        return dict(program=PROGRAM_SSSP, g=g, source=0, init=P.sssp_init(g.n_vertices, 0),
+        g = gen_grid(1024, SEED, source=source)
+        init = np.full(g.n_vertices, unreached, np.int32)
+        init[0] = 0
+        return dict(program=2, g=g, source=0, init=init,
                     active=(0, g.n_vertices), max_iters=0, vd_bytes=4, ed_bytes=4, gather=True)
     if name == "bfs-rmat16":
-        g = graphs.rmat(16, 16, seed=SEED, symmetrize=True)
-        s = P.max_outdegree_vertex(g.n_vertices, g.srcs)
-        return dict(program=PROGRAM_BFS, g=g, source=s, init=P.bfs_init(g.n_vertices),
+        g = gen_rmat(16, SEED, symmetrize=True, source=source)
+        s = max_outdegree_vertex(g.n_vertices, g.srcs)
+        return dict(program=1, g=g, source=s, init=np.full(g.n_vertices, -1, np.int32),
                     active=(s, s + 1), max_iters=0, vd_bytes=4, ed_bytes=0, gather=False)
     if name == "pagerank-rmat22":
-        g = graphs.rmat(RMAT_SCALE[name], 16, seed=SEED)
-        return dict(program=PROGRAM_PAGERANK, g=g, source=0, init=P.pagerank_init(g.n_vertices, g.srcs),
+        g = gen_rmat(RMAT_SCALE[name], SEED, source=source)
+        init = np.zeros(g.n_vertices, dtype=[("rank", np.float32), ("numOutEdges", np.int32)])
+        init["rank"] = np.float32(0.15)
+        init["numOutEdges"] = np.bincount(g.srcs, minlength=g.n_vertices)
+        return dict(program=4, g=g, source=0, init=init,
                     active=(0, g.n_vertices), max_iters=50, vd_bytes=8, ed_bytes=0, gather=True)
     if name == "cc-rmat22":
-        g = graphs.rmat(RMAT_SCALE[name], 16, seed=SEED, symmetrize=True)
-        return dict(program=PROGRAM_CC, g=g, source=0, init=P.cc_init(g.n_vertices),
+        g = gen_rmat(RMAT_SCALE[name], SEED, symmetrize=True, source=source)
+        return dict(program=3, g=g, source=0, init=np.arange(g.n_vertices, dtype=np.int32),
                     active=(0, g.n_vertices), max_iters=0, vd_bytes=4, ed_bytes=0, gather=True)
     raise SystemExit(f"unknown workload {name}")
+
+
+def workload_config(name: str, g=None) -> dict:
+    """The `config` object of a workload: identical in both arms."""
+    cfg = {"workload": name, "desc": WORKLOADS[name]["desc"], "seed": SEED}
+    if g is not None:
+        cfg.update(n_vertices=g.n_vertices, n_edges=g.n_edges)
+        if name in RMAT_SCALE:
+            cfg["rmat_scale"] = RMAT_SCALE[name]
+    return cfg
 
 
 def round_bytes(st: dict, vd: int, ed: int, gather: bool):
@@ -119,6 +185,20 @@ def measured_peak() -> tuple[float, str]:
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def mapped_libraries() -> list[str]:
+    """Shared libraries of this repository mapped into this process."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                p = line.split()[-1] if line.strip() else ""
+                if p.startswith(ROOT) and ".so" in p:
+                    out.add(os.path.relpath(p, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
 
 
 class ClockSampler:
@@ -185,7 +265,8 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("gloo")
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
     return world, rank, local
 
 
@@ -215,19 +296,44 @@ def allreduce_sum(world, x: float) -> float:
     return float(t.item())
 
 
-def cpu_run(engine, w, name):
+def cpu_run(engine, w, name, fp64=False):
+    """One oracle run of a plain workload: (result, stats)."""
     g = w["g"]
     if name == "sssp-grid1024":
-        _, st = engine.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, w["source"], stats_cap=1 << 14)
-    elif name == "bfs-rmat16":
-        _, st = engine.bfs(g.n_vertices, g.srcs, g.dsts, w["source"], stats_cap=1 << 14)
-    elif name == "pagerank-rmat22":
-        _, st = engine.pagerank(g.n_vertices, g.srcs, g.dsts, max_iters=50, stats_cap=1 << 14)
-    else:
-        _, st = engine.cc(g.n_vertices, g.srcs, g.dsts, stats_cap=1 << 14)
-    return st
+        return engine.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, w["source"], stats_cap=1 << 14)
+    if name == "bfs-rmat16":
+        return engine.bfs(g.n_vertices, g.srcs, g.dsts, w["source"], stats_cap=1 << 14)
+    if name == "pagerank-rmat22":
+        return engine.pagerank(g.n_vertices, g.srcs, g.dsts, max_iters=50, fp64=fp64,
+                               stats_cap=1 << 14)
+    return engine.cc(g.n_vertices, g.srcs, g.dsts, stats_cap=1 << 14)
 
 
+def in_threads(*fns):
+    """Runs the callables at once on host threads (ctypes calls drop the
+    GIL) and returns their results in order."""
+    out = [None] * len(fns)
+
+    def run(i, f):
+        out[i] = f()
+    ts = [threading.Thread(target=run, args=(i, f)) for i, f in enumerate(fns)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return out
+
+
+def pr_error(got: np.ndarray, ref64: np.ndarray) -> dict:
+    """FP32 PageRank against the FP64 oracle: relative L1 and the largest
+    per-vertex relative error."""
+    a, b = got.astype(np.float64), ref64.astype(np.float64)
+    rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+    return {"rel_l1_vs_fp64": float(np.abs(a - b).sum() / np.abs(b).sum()),
+            "max_rel_err_vs_fp64": float(rel.max()), "bound_rel_l1": 1e-5}
+
+
+# ---------------------------------------------------------------- C5 / C4 --
 C5_GRAPHS = [("rmat12", 12), ("rmat14", 14), ("rmat16", 16), ("rmat18", 18), ("rmat20", 20),
              ("rmat21", 21), ("rmat22", 22), ("grid1024", None)]
 C5_MIX = (0.5, 0.3, 0.2)      # BFS / SSSP / PPR
@@ -237,41 +343,32 @@ C5_SWEEP_QUERIES = 512
 C5_LANES = 8                  # batches in flight at once
 
 
-def c5_graphs(only=None):
-    from vertexapi2_gb300 import graphs
+def c5_graphs(only=None, source="product"):
     out = []
     for name, sc in C5_GRAPHS:
         if only and name not in only:
             continue
         if sc is None:
-            g = graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100))
+            g = gen_grid(1024, SEED, source=source)
         else:
-            g = graphs.rmat(sc, 16, seed=SEED + sc, symmetrize=True, weights=(1, 255))
+            g = gen_rmat(sc, SEED + sc, symmetrize=True, weights=(1, 255), source=source)
         out.append((name, g))
     return out
+
+
+def c4_graphs(scale=21, side=1024, source="product"):
+    return [(f"rmat{scale}", gen_rmat(scale, SEED, symmetrize=True, weights=(1, 255), source=source)),
+            (f"grid{side}", gen_grid(side, SEED, source=source))]
 
 
 def query_mix(gs, n, seed, mix=C5_MIX):
     """n (graph index, program, source) triples: programs drawn from `mix`
     (BFS/SSSP/PPR), graph and source uniform."""
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
     rng = np.random.default_rng(seed)
-    progs = rng.choice([PROGRAM_BFS, PROGRAM_SSSP, PROGRAM_PPR], size=n, p=list(mix))
+    progs = rng.choice([1, 2, 5], size=n, p=list(mix))
     gids = rng.integers(0, len(gs), n)
     srcs = [int(rng.integers(0, gs[k][1].n_vertices)) for k in gids]
     return list(zip(gids.tolist(), progs.tolist(), srcs))
-
-
-def c4_queries(gs, nq=256):
-    """batch-c4's queries: nq BFS + nq SSSP sources per graph (seeded as the
-    batched leg draws them)."""
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
-    rng = np.random.default_rng(SEED)
-    out = []
-    for k, (_, g) in enumerate(gs):
-        for prog in (PROGRAM_BFS, PROGRAM_SSSP):
-            out += [(k, prog, int(s)) for s in rng.integers(0, g.n_vertices, nq)]
-    return out
 
 
 def cpu_cells(gs, cells, threads, per_cell=1, seed=SEED + 11):
@@ -289,7 +386,6 @@ def cpu_cells(gs, cells, threads, per_cell=1, seed=SEED + 11):
     Returns (queries/s, queries run, wall s, engine kind)."""
     import queue
     import oracle
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
     port = oracle.port()
     eng = oracle.ref() or port
     rng = np.random.default_rng(seed)
@@ -308,9 +404,9 @@ def cpu_cells(gs, cells, threads, per_cell=1, seed=SEED + 11):
             except queue.Empty:
                 return
             g = gs[k][1]
-            if p == PROGRAM_BFS:
+            if p == 1:
                 _, st = eng.bfs(g.n_vertices, g.srcs, g.dsts, s0)
-            elif p == PROGRAM_SSSP:
+            elif p == 2:
                 _, st = eng.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, s0)
             else:
                 _, st = port.ppr(g.n_vertices, g.srcs, g.dsts, s0, iters=20)
@@ -329,105 +425,88 @@ def cpu_cells(gs, cells, threads, per_cell=1, seed=SEED + 11):
 
 
 def c5_cells(gs):
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
-    progs = dict(zip((PROGRAM_BFS, PROGRAM_SSSP, PROGRAM_PPR), C5_MIX))
+    progs = dict(zip((1, 2, 5), C5_MIX))
     return {(k, p): w / len(gs) for k in range(len(gs)) for p, w in progs.items()}
 
 
 def c4_cells(gs):
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
-    return {(k, p): 1.0 / (2 * len(gs)) for k in range(len(gs)) for p in (PROGRAM_BFS, PROGRAM_SSSP)}
+    return {(k, p): 1.0 / (2 * len(gs)) for k in range(len(gs)) for p in (1, 2)}
 
 
-def run_reference_queries(args):
-    """Reference arm of the query workloads: the CPU engines on every host
-    core over a bounded sample of the workload's queries."""
-    world, rank, _ = dist_setup()
-    if rank != 0:
-        return
-    cores = os.cpu_count() or 1
-    if args.workload == "batch-c4":
-        from vertexapi2_gb300 import graphs
-        gs = [("rmat21", graphs.rmat(21, 16, seed=SEED, symmetrize=True, weights=(1, 255))),
-              ("grid1024", graphs.grid(1024, 1024, 0.15, seed=SEED, weights=(1, 100)))]
-        cells = c4_cells(gs)
-        metric = "batched queries/s (vs one-at-a-time plain engine)"
-    else:
-        gs = c5_graphs()
-        cells = c5_cells(gs)
-        metric = "served queries/s, p50/p99 latency (vs one-at-a-time plain engine)"
-    per_cell = max(1, -(-cores // len(cells)))
-    value, n, wall, kind = cpu_cells(gs, cells, cores, per_cell)
-    line = {
-        "impl": "reference", "metric": metric, "value": value, "unit": "queries/s",
-        "n_gpus": args.gpus, "steps": 1, "warmup": 0,
-        "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"], "seed": SEED},
-        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": kind,
-                         "sample": f"one step (of the {args.steps} asked; a cell of the largest graph "
-                                   f"runs for minutes on one core): {per_cell} random source(s) per "
-                                   f"(graph, program) cell, {n} queries on {cores} threads in "
-                                   f"{wall:.0f} s; value = {cores} / (mix-weighted mean run() time); "
-                                   f"BFS/SSSP on the {kind} engine, PPR on the restatement"},
-        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line))
-
-
+# --------------------------------------------------------- reference arm --
 def run_reference(args):
-    """CPU reference engine on every host core (rank 0 only)."""
-    if args.workload in ("batch-c4", "serve-c5"):
-        return run_reference_queries(args)
+    """The reference's CPU engine on every host core (rank 0 only), on the
+    headline workload (or the one --workload names).  Graphs come from the
+    oracle's generators: the product library is never loaded here."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
     import oracle
-    eng = oracle.ref() or oracle.port()
-    w = make_workload(args.workload)
-    port = oracle.port()
-    # traversed edges per run (from the restatement's instrumented counts)
-    st = cpu_run(port, w, args.workload)
-    edges = float(st["gathered"].sum() + st["scattered"].sum())
     cores = os.cpu_count() or 1
+    port = oracle.port()
+    eng = oracle.ref() or port
+    if args.workload in ("batch-c4", "serve-c5"):
+        if args.workload == "batch-c4":
+            gs = c4_graphs(source="oracle")
+            cells = c4_cells(gs)
+            metric = "batched queries/s (vs one-at-a-time plain engine)"
+        else:
+            gs = c5_graphs(source="oracle")
+            cells = c5_cells(gs)
+            metric = "served queries/s, p50/p99 latency (vs one-at-a-time plain engine)"
+        per_cell = max(1, -(-cores // len(cells)))
+        value, n, wall, kind = cpu_cells(gs, cells, cores, per_cell)
+        sample = (f"one step (of the {args.steps} asked; a cell of the largest graph runs for "
+                  f"minutes on one core): {per_cell} random source(s) per (graph, program) cell, "
+                  f"{n} queries on {cores} threads in {wall:.0f} s; value = {cores} / (mix-weighted "
+                  f"mean run() time); BFS/SSSP on the {kind} engine, PPR on the restatement")
+        line = {"metric": metric, "value": value, "unit": "queries/s", "steps": 1, "warmup": 0,
+                "ms_per_step": 1e3 * wall, "config": workload_config(args.workload),
+                "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores,
+                                 "kind": kind, "sample": sample}}
+    else:
+        w = make_workload(args.workload, source="oracle")
+        # traversed edges per run (from the restatement's instrumented counts)
+        _, st = cpu_run(port, w, args.workload)
+        edges = float(st["gathered"].sum() + st["scattered"].sum())
 
-    def one_step():
-        ts = [threading.Thread(target=cpu_run, args=(eng, w, args.workload)) for _ in range(cores)]
-        t0 = time.perf_counter()
-        for t in ts:
-            t.start()
-        for t in ts:
-            t.join()
-        return time.perf_counter() - t0
+        def one_step():
+            t0 = time.perf_counter()
+            in_threads(*[lambda: cpu_run(eng, w, args.workload)] * cores)
+            return time.perf_counter() - t0
 
-    for _ in range(args.warmup):
-        one_step()
-    times = [one_step() for _ in range(args.steps)]
-    total = sum(times)
-    value = cores * edges * args.steps / total / 1e9
-    line = {
-        "impl": "reference", "metric": "GTEPS & %HBM roofline per algo", "value": value,
-        "unit": "GTEPS", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        for _ in range(args.warmup):
+            one_step()
+        times = [one_step() for _ in range(args.steps)]
+        total = sum(times)
+        value = cores * edges * args.steps / total / 1e9
+        line = {"metric": "GTEPS & %HBM roofline per algo", "value": value, "unit": "GTEPS",
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+                "config": workload_config(args.workload, w["g"]),
+                "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": eng.kind,
+                                 "sample": f"{cores} concurrent full runs of the workload per step "
+                                           f"({st['iterations']} rounds each)"}}
+    libs = mapped_libraries()
+    if any("libgas_gb300" in p for p in libs):
+        raise SystemExit(f"reference arm mapped the product library: {libs}")
+    unit = line["unit"]
+    line.update({
+        "impl": "reference", "n_gpus": args.gpus, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
-                   "n_vertices": w["g"].n_vertices, "n_edges": w["g"].n_edges, "seed": SEED},
-        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": eng.kind,
-                         "sample": f"{cores} concurrent full runs of the workload per step"},
-        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+        "e2e": {"value": line["value"], "unit": unit, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "native_libraries": libs,
+    })
     print(json.dumps(line))
 
 
-def run_ours(args):
-    world, rank, local = dist_setup()
+# ------------------------------------------------------- plain workloads --
+def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
+    """One plain-engine workload: device-timed GTEPS, e2e through the C ABI,
+    roofline of the run's kernels, CPU baseline and oracle parity."""
     import torch
-    torch.cuda.set_device(local)
     import vertexapi2_gb300 as gas
-    gas.load()
-    if not gas.device_supported(local):
-        raise SystemExit(f"cuda:{local} is not an sm_103 device")
-    w = make_workload(args.workload)
+    w = make_workload(name)
     g = w["g"]
     stream = torch.cuda.current_stream()
     eng = gas.GASEngine(w["program"], device=local, stream=stream.cuda_stream)
@@ -444,7 +523,7 @@ def run_ours(args):
         eng.set_active(lo, hi)
         return eng.run(w["max_iters"])
 
-    for _ in range(max(args.warmup, 1)):
+    for _ in range(max(warmup, 1)):
         rounds = device_step()
     stats = eng.round_stats()
     edges_per_run = float(stats["gathered"].sum() + stats["scattered"].sum())
@@ -457,26 +536,26 @@ def run_ours(args):
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
+          for _ in range(steps)]
     barrier(world)
     torch.cuda.synchronize()
     run_kernel_ms = 0.0
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
-        for k in range(args.steps):
+        for k in range(steps):
             flush.fill_(k)                      # L2 flush between timed steps
             eng.restore_vertex_data()
             ev[k][0].record(stream)
             eng.set_active(lo, hi)
             eng.run(w["max_iters"])
             ev[k][1].record(stream)
-            run_kernel_ms += eng.last_run_ms()  # the run kernel's own events
+            run_kernel_ms += eng.last_run_ms()  # the run kernels' own events
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     barrier(world)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = allreduce_max(world, float(sum(step_ms)))
-    all_edges = allreduce_sum(world, edges_per_run * args.steps)
+    all_edges = allreduce_sum(world, edges_per_run * steps)
     value = all_edges / (total_ms / 1e3) / 1e9
 
     # end to end through the C ABI with host buffers: initial vertex data
@@ -485,7 +564,7 @@ def run_ours(args):
     result = torch.empty(init.nbytes, dtype=torch.uint8).pin_memory().numpy().view(init.dtype)
     e2e_eng = gas.GASEngine(w["program"], device=local, stream=stream.cuda_stream)
     e2e_eng.set_graph(g.n_vertices, result, g.srcs, g.dsts, ed)
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         e2e_eng.set_vertex_data(host_in)
         e2e_eng.set_active(lo, hi)
         e2e_eng.run(w["max_iters"])
@@ -493,7 +572,7 @@ def run_ours(args):
     barrier(world)
     torch.cuda.synchronize()
     e2e_local = 0.0
-    for k in range(args.steps):
+    for k in range(steps):
         flush.fill_(k)  # L2 flushed before each step, as for the device-timed steps
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -506,135 +585,136 @@ def run_ours(args):
     e2e_s = allreduce_max(world, e2e_local)
     e2e_value = all_edges / e2e_s / 1e9
     eng.get_results()  # device-resident run's result, into `init`
-    if init.dtype.names:  # FP programs: sums depend on frontier order
-        a, b = init["rank"].astype(np.float64), result["rank"].astype(np.float64)
-        if np.abs(a - b).sum() > 1e-5 * np.abs(b).sum():
-            raise SystemExit("end-to-end result differs from the device-resident run")
-    elif not np.array_equal(init, result):
-        raise SystemExit("end-to-end result differs from the device-resident run")
+    e2e_eng.close()
+    eng.close()
+    del flush
     nbytes = init.nbytes
 
     peak, peak_kind = measured_peak()
-    gms, sms_ = kt["gather_ms"], kt["scatter_ms"]
-    # run() is one persistent kernel: its bytes are every round's gather and
-    # scatter bytes, its time the CUDA events around its launch
     run_bytes = float(gbytes.sum() + sbytes.sum())
-    kernel_ms = run_kernel_ms / args.steps
+    kernel_ms = run_kernel_ms / steps
     achieved = run_bytes / (kernel_ms / 1e3) / 1e9 if kernel_ms > 0 else 0.0
     # range split + (leading dense-rounds kernel when every vertex starts
     # active) + persistent run
     dense_first = (lo, hi) == (0, g.n_vertices)
     launches_per_step = 1 + (1 if w["gather"] else 0) + (1 if dense_first else 0)
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
+    # CPU baseline (one core, the restatement) and parity with the oracle
+    cpu, parity = None, None
+    if rank == 0 and with_cpu:
         import oracle
         port = oracle.port()
         t0 = time.perf_counter()
-        st = cpu_run(port, w, args.workload)
+        if w["program"] == 4:  # FP32 baseline and the FP64 oracle side by side
+            (ref, st), (ref64, _) = in_threads(lambda: cpu_run(port, w, name),
+                                               lambda: cpu_run(port, w, name, fp64=True))
+        else:
+            ref, st = cpu_run(port, w, name)
         cpu_s = time.perf_counter() - t0
         cpu_edges = float(st["gathered"].sum() + st["scattered"].sum())
         cpu = {"value": cpu_edges / (st["run_ns"] / 1e9) / 1e9, "unit": "GTEPS", "cores": 1,
                "kind": "port",
                "sample": f"one full run of the workload ({st['iterations']} rounds, "
                          f"{cpu_s:.1f} s wall), run()+getResults() timed as bfs.cu:100-111"}
-    if rank != 0:
-        return
-    clocks = clk.summary()
-    line = {
+        same_rounds = st["iterations"] == rounds
+        if w["program"] == 4:
+            parity = dict(pr_error(init["rank"], ref64), vs="oracle FP64 PageRank (same graph)",
+                          e2e_rel_l1_vs_fp64=pr_error(result["rank"], ref64)["rel_l1_vs_fp64"],
+                          rounds_equal=bool(same_rounds))
+            parity["ok"] = bool(parity["rel_l1_vs_fp64"] <= 1e-5 and
+                                parity["e2e_rel_l1_vs_fp64"] <= 1e-5)
+        else:
+            ok = bool(np.array_equal(init, ref) and np.array_equal(result, ref))
+            parity = {"vs": "oracle (same graph)", "bit_exact": ok, "rounds_equal": bool(same_rounds),
+                      "ok": ok and bool(same_rounds)}
+    return {
         "metric": "GTEPS & %HBM roofline per algo", "value": value, "unit": "GTEPS",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32" if w["program"] != 4 else "f32",
+        "n_gpus": world, "steps": steps, "warmup": warmup,
+        "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if w["program"] == 4 else "int32",
         "data": "synthetic",
-        "config": {"workload": args.workload, "desc": WORKLOADS[args.workload]["desc"],
-                   "rmat_scale": RMAT_SCALE.get(args.workload), "n_vertices": g.n_vertices, "n_edges": g.n_edges, "seed": SEED,
-                   "rounds": rounds, "edges_traversed_per_run": edges_per_run,
-                   "l2": "flushed before every timed step, device-timed and end-to-end (512 MB write)",
-                   "parallelism": f"replicas x{world}",
-                   "set_graph_ms": set_graph_ms},
+        "config": workload_config(name, g),
+        "run": {"rounds": rounds, "edges_traversed_per_run": edges_per_run,
+                "l2": "flushed before every timed step, device-timed and end-to-end (512 MB write)",
+                "parallelism": f"replicas x{world}", "set_graph_ms": set_graph_ms},
         "roofline": {"bound": "hbm",
                      "kernel": "run_dense_kernel + run_persistent_kernel" if dense_first
                      else "run_persistent_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
-                     "traffic": (TRAFFIC_PER_LAUNCH.get(args.workload)
-                                 if RMAT_SCALE.get(args.workload, 22) == 22 else None),
+                     "traffic": (TRAFFIC_PER_LAUNCH.get(name)
+                                 if RMAT_SCALE.get(name, 22) == 22 else None),
                      "kernel_ms_per_launch": kernel_ms,
                      "algorithmic_bytes_per_launch": run_bytes,
                      "phase_profile_per_launch_kernels": {
-                         "gather_apply_ms": gms, "scatter_activate_ms": sms_,
+                         "gather_apply_ms": kt["gather_ms"], "scatter_activate_ms": kt["scatter_ms"],
                          "gather_apply_bytes": float(gbytes.sum()),
                          "scatter_activate_bytes": float(sbytes.sum())}},
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": {"value": e2e_value, "unit": "GTEPS", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "ms_per_step": 1e3 * e2e_s / args.steps},
-        "gpu_launches": launches_per_step * args.steps,
-        "clocks": clocks,
+                "d2h_bytes_per_step": nbytes, "ms_per_step": 1e3 * e2e_s / steps},
+        "gpu_launches": launches_per_step * steps,
+        "clocks": clk.summary(),
         "wall_s_timed": wall,
     }
-    print(json.dumps(line))
 
 
-def run_batch_c4(args):
-    """Batched multi-source queries (queries/s) vs one-at-a-time plain runs."""
-    world, rank, local = dist_setup()
+# ------------------------------------------------------------------- C4 --
+def measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu=True):
+    """Batched multi-source queries (queries/s) vs one-at-a-time plain runs,
+    with a sample of every set checked against the oracle."""
     import torch
-    torch.cuda.set_device(local)
     import vertexapi2_gb300 as gas
-    from vertexapi2_gb300 import graphs
-    from vertexapi2_gb300 import programs as P
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_SSSP
-    gas.load()
     stream = torch.cuda.current_stream()
     rng = np.random.default_rng(SEED)
     nq = 256
-    sc, side = args.rmat_scale or 21, args.grid_side
-    gs = [(f"rmat{sc}", graphs.rmat(sc, 16, seed=SEED, symmetrize=True, weights=(1, 255))),
-          (f"grid{side}", graphs.grid(side, side, 0.15, seed=SEED, weights=(1, 100)))]
+    gs = c4_graphs(args.rmat_scale or 21, args.grid_side)
     only = set(args.c4_sets.split(",")) if args.c4_sets else None
-    sets = []
+    sets, batches = [], []
     for name, g in gs:
         b = gas.GASBatch(device=local, stream=stream.cuda_stream)
         b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
-        for prog in (PROGRAM_BFS, PROGRAM_SSSP):
+        batches.append(b)
+        for prog in (1, 2):
             src = rng.integers(0, g.n_vertices, nq).astype(np.int32)
-            key = f"{name}-{'bfs' if prog == PROGRAM_BFS else 'sssp'}"
+            key = f"{name}-{PROGRAM_NAMES[prog]}"
             if only is not None and key not in only:
                 continue
             if args.no_autotune:
-                cfg = (256, 0, args.c4_delta if prog == PROGRAM_SSSP else 0)
+                cfg = (256, 0, args.c4_delta if prog == 2 else 0)
             else:
-                cfg = b.autotune(prog, nq) + (b.get_delta() if prog == PROGRAM_SSSP else 0,)
-            sets.append((name, g, b, prog, src, cfg))
+                cfg = b.autotune(prog, nq) + (b.get_delta() if prog == 2 else 0,)
+            sets.append((key, g, b, prog, src, cfg))
     per_set_ms = [0.0] * len(sets)
     per_set_rounds = [0] * len(sets)
 
     def batched_step():
         ms = 0.0
-        for i, (name, g, b, prog, src, cfg) in enumerate(sets):
+        for i, (key, g, b, prog, src, cfg) in enumerate(sets):
             b.set_config(cfg[0], cfg[1], True)
             b.set_delta(cfg[2])
             _, per_set_rounds[i] = b.run(prog, src, want_results=False)
             ms += b.last_ms()
             per_set_ms[i] += b.last_ms()
         return ms
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batched_step()
     barrier(world)
     torch.cuda.synchronize()
     per_set_ms[:] = [0.0] * len(sets)
     with ClockSampler(local) as clk:
-        step_ms = [batched_step() for _ in range(args.steps)]
+        step_ms = [batched_step() for _ in range(steps)]
     total_ms = allreduce_max(world, float(sum(step_ms)))
-    queries = allreduce_sum(world, float(len(sets) * nq * args.steps))
+    queries = allreduce_sum(world, float(len(sets) * nq * steps))
     value = queries / (total_ms / 1e3)
-    # end to end: results of every query copied to host memory each step
+    # end to end: sources up and every query's result copied to host memory
     t0 = time.perf_counter()
-    for name, g, b, prog, src, cfg in sets:
+    outs = []
+    for key, g, b, prog, src, cfg in sets:
         b.set_config(cfg[0], cfg[1], True)
         b.set_delta(cfg[2])
-        b.run(prog, src, want_results=True)
+        outs.append(b.run(prog, src, want_results=True)[0])
     e2e_s = time.perf_counter() - t0
     e2e_value = len(sets) * nq / e2e_s
     d2h = sum(nq * g.n_vertices * 4 for _, g, _, _, _, _ in sets)
@@ -643,61 +723,86 @@ def run_batch_c4(args):
     single_ms, single_n = 0.0, 0
     parity = True
     per_set = {}
-    for i, (name, g, b, prog, src, cfg) in enumerate(sets):
+    for i, (key, g, b, prog, src, cfg) in enumerate(sets):
         s_ms0 = single_ms
-        b.set_config(cfg[0], cfg[1], True)
-        b.set_delta(cfg[2])
-        batch_out, _ = b.run(prog, src[:sample])
         e = gas.GASEngine(prog, device=local, stream=stream.cuda_stream)
         for q, s0 in enumerate(src[:sample]):
-            vd = P.bfs_init(g.n_vertices) if prog == PROGRAM_BFS else P.sssp_init(g.n_vertices, int(s0))
-            e.set_graph(g.n_vertices, vd, g.srcs, g.dsts, g.weights if prog == PROGRAM_SSSP else None) \
+            if prog == 1:
+                vd = np.full(g.n_vertices, -1, np.int32)
+            else:
+                vd = np.full(g.n_vertices, 2**31 - 1 - 100000, np.int32)
+                vd[int(s0)] = 0
+            e.set_graph(g.n_vertices, vd, g.srcs, g.dsts, g.weights if prog == 2 else None) \
                 if q == 0 else e.set_vertex_data(vd)
-            act = (int(s0), int(s0) + 1) if prog == PROGRAM_BFS else (0, g.n_vertices)
+            act = (int(s0), int(s0) + 1) if prog == 1 else (0, g.n_vertices)
             e.set_active(*act)
             e.run()
             single_ms += e.last_run_ms()
             single_n += 1
             e.get_results()  # into the array borrowed by set_graph
-            parity &= bool(np.array_equal(e.vertex_data, batch_out[q]))
+            parity &= bool(np.array_equal(e.vertex_data, outs[i][q]))
         e.close()
-        key = f"{name}-{'bfs' if prog == PROGRAM_BFS else 'sssp'}"
-        per_set[key] = {"batched_ms_per_256": per_set_ms[i] / args.steps,
+        per_set[key] = {"batched_ms_per_256": per_set_ms[i] / steps,
                         "batched_rounds": per_set_rounds[i],
                         "single_ms": (single_ms - s_ms0) / sample,
-                        "speedup": ((single_ms - s_ms0) / sample * nq) / (per_set_ms[i] / args.steps)}
+                        "speedup": ((single_ms - s_ms0) / sample * nq) / (per_set_ms[i] / steps)}
+    for b in batches:
+        b.close()
     single_qps = single_n / (single_ms / 1e3)
-    if rank != 0:
-        return
-    line = {
+    # oracle parity on a sample of every set (two queries per set, at once)
+    oracle_ok, oracle_n, cpu = None, 0, None
+    if rank == 0 and with_cpu:
+        import oracle
+        port = oracle.port()
+        jobs = []
+        for i, (key, g, b, prog, src, cfg) in enumerate(sets):
+            for q in (0, nq - 1):
+                if prog == 1:
+                    jobs.append((i, q, lambda g=g, s0=int(src[q]): port.bfs(g.n_vertices, g.srcs, g.dsts, s0)[0]))
+                else:
+                    jobs.append((i, q, lambda g=g, s0=int(src[q]): port.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, s0)[0]))
+        res = in_threads(*[f for _, _, f in jobs])
+        oracle_ok = all(np.array_equal(r, outs[i][q]) for (i, q, _), r in zip(jobs, res))
+        oracle_n = len(jobs)
+        cores = os.cpu_count() or 1
+        cells = c4_cells(gs)
+        v, n, wall, kind = cpu_cells(gs, cells, cores, max(1, -(-cores // len(cells))))
+        cpu = {"value": v, "unit": "queries/s", "cores": cores, "kind": kind,
+               "sample": f"{n} random sources spread over the (graph, program) cells on {cores} "
+                         f"threads in {wall:.0f} s; value = {cores} / (mean run() time per query "
+                         f"of the mix)"}
+    return {
         "metric": "batched queries/s (vs one-at-a-time plain engine)", "value": value,
-        "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "unit": "queries/s", "n_gpus": world, "steps": steps, "warmup": warmup,
+        "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": "batch-c4", "desc": WORKLOADS["batch-c4"]["desc"], "seed": SEED,
-                   "queries_per_step": len(sets) * nq,
-                   "autotuned": {f"{n}-{'bfs' if p == PROGRAM_BFS else 'sssp'}": list(c)
-                                 for n, _, _, p, _, c in sets},
-                   "l2": "inputs (R-MAT-21 CSC/CSR, 2 GB query state) larger than L2"},
+        "config": workload_config("batch-c4"),
+        "run": {"queries_per_step": len(sets) * nq,
+                "autotuned": {k: list(c) for k, _, _, _, _, c in sets},
+                "l2": "inputs (R-MAT-21 CSC/CSR, 2 GB query state) larger than L2"},
         "one_at_a_time": {"value": single_qps, "unit": "queries/s", "sample_queries": single_n,
                           "speedup": value / single_qps, "results_identical": parity},
         "per_set": per_set,
+        "parity": {"vs": "oracle BFS/SSSP on the first and last source of every set",
+                   "queries": oracle_n, "bit_exact": oracle_ok,
+                   "ok": bool(oracle_ok and parity) if oracle_ok is not None else None},
+        "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * nq * len(sets),
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": 5 * len(sets) * args.steps,
+        "gpu_launches": 5 * len(sets) * steps,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line))
 
 
-def serve_pass(srv, ids, gs, queries, rate, bufs, seed):
+# ------------------------------------------------------------------- C5 --
+def serve_pass(srv, ids, gs, queries, rate, bufs, seed, keep=None):
     """Submits `queries` with Poisson arrivals at `rate` queries/s (inf: all
     at once) from a submitter thread while this thread waits for each result
-    in submission order and copies it into the graph's pinned buffer.
+    in submission order and copies it into the graph's pinned buffer (and a
+    copy of it into `keep[i]` for the indices `keep` holds).
     Returns per-query infos and the wall time from the first submission to
     the last result in host memory."""
     import queue
-    from vertexapi2_gb300._lib import PROGRAM_PPR
     n = len(queries)
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n)) if np.isfinite(rate) else np.zeros(n)
@@ -721,7 +826,10 @@ def serve_pass(srv, ids, gs, queries, rate, bufs, seed):
     for _ in range(n):
         i, t = handoff.get()
         k, p, _ = queries[i]
-        _, infos[i] = srv.wait(t, out=bufs[k][1 if p == PROGRAM_PPR else 0])
+        out = bufs[k][1 if p == 5 else 0]
+        _, infos[i] = srv.wait(t, out=out)
+        if keep is not None and i in keep:
+            keep[i] = out.copy()
     wall = time.perf_counter() - t0
     th.join()
     bad = [x for x in infos if x["status"] != 0]
@@ -737,10 +845,9 @@ def serve_summary(infos, gs=None):
            "p99_ms": float(np.percentile(lat, 99)), "span_s": span,
            "mean_batch": float(np.mean([x["batchSize"] for x in infos]))}
     if gs is not None:  # p50 latency and rounds per graph and program
-        names = {1: "bfs", 2: "sssp", 5: "ppr"}
         cells, batches = {}, {}
         for x, l in zip(infos, lat):
-            key = f"{gs[x['graph']][0]}-{names[x['program']]}"
+            key = f"{gs[x['graph']][0]}-{PROGRAM_NAMES[x['program']]}"
             cells.setdefault(key, []).append((l, x["rounds"], (x["doneNs"] - x["admitNs"]) / 1e6))
             batches.setdefault(key, {})[(x["lane"], x["admitNs"])] = (x["doneNs"] - x["admitNs"]) / 1e6
         # lane_ms: the cell's batches' run times summed (lane time it held)
@@ -769,52 +876,91 @@ def plain_one_at_a_time(gs, local, stream, per_cell=4):
     results do."""
     import vertexapi2_gb300 as gas
     from vertexapi2_gb300 import programs as P
-    from vertexapi2_gb300._lib import PROGRAM_BFS, PROGRAM_PPR, PROGRAM_SSSP
     rng = np.random.default_rng(SEED + 3)
     cells, results = {}, []
     for k, (name, g) in enumerate(gs):
-        for prog in (PROGRAM_BFS, PROGRAM_SSSP, PROGRAM_PPR):
+        for prog in (1, 2, 5):
             srcs = [int(x) for x in rng.integers(0, g.n_vertices, per_cell)]
             e = gas.GASEngine(prog, device=local, stream=stream)
             times = []
             for q, s0 in enumerate(srcs):
-                if prog == PROGRAM_BFS:
+                if prog == 1:
                     vd, act = P.bfs_init(g.n_vertices), (s0, s0 + 1)
-                elif prog == PROGRAM_SSSP:
+                elif prog == 2:
                     vd, act = P.sssp_init(g.n_vertices, s0), (0, g.n_vertices)
                 else:
                     vd, act = P.ppr_init(g.n_vertices, g.srcs, s0), (0, g.n_vertices)
                 vd = pinned_like(vd)
                 if q == 0:  # the engine borrows a page-locked result array
                     e.set_graph(g.n_vertices, pinned_like(vd), g.srcs, g.dsts,
-                                g.weights if prog == PROGRAM_SSSP else None)
+                                g.weights if prog == 2 else None)
                 else:
                     e.set_vertex_data(vd)
                 e.set_active(*act)
-                e.run(20 if prog == PROGRAM_PPR else 0)   # warm
+                e.run(20 if prog == 5 else 0)   # warm
                 e.set_vertex_data(vd)
                 t0 = time.perf_counter()
                 e.set_active(*act)
-                e.run(20 if prog == PROGRAM_PPR else 0)
+                e.run(20 if prog == 5 else 0)
                 e.get_results()
                 times.append(time.perf_counter() - t0)
-                res = e.vertex_data["rank"].copy() if prog == PROGRAM_PPR else e.vertex_data.copy()
+                res = e.vertex_data["rank"].copy() if prog == 5 else e.vertex_data.copy()
                 results.append((k, prog, s0, res))
             e.close()
             cells[(k, prog)] = float(np.mean(times))
-    mix = {PROGRAM_BFS: C5_MIX[0], PROGRAM_SSSP: C5_MIX[1], PROGRAM_PPR: C5_MIX[2]}
+    mix = dict(zip((1, 2, 5), C5_MIX))
     expected = sum(cells[(k, p)] * mix[p] / len(gs) for (k, p) in cells)
     return 1.0 / expected, cells, results
 
 
-def run_serve_c5(args):
+def c5_oracle_check(gs, queries, kept):
+    """Served results of a sample of the mix against the oracle, at once on
+    host threads: BFS/SSSP bit for bit; PPR within 1e-5 relative L1 of the
+    FP64 oracle, and bit for bit with the FP32 oracle on graphs whose
+    in-degrees are all <= 4096 (the served sums follow its order there)."""
+    import oracle
+    port = oracle.port()
+    jobs = []
+    for i in sorted(kept):
+        k, p, s0 = queries[i]
+        g = gs[k][1]
+        if p == 1:
+            jobs.append(lambda g=g, s0=s0: port.bfs(g.n_vertices, g.srcs, g.dsts, s0)[0])
+        elif p == 2:
+            jobs.append(lambda g=g, s0=s0: port.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, s0)[0])
+        else:
+            jobs.append(lambda g=g, s0=s0: (port.ppr(g.n_vertices, g.srcs, g.dsts, s0, iters=20)[0],
+                                            port.ppr(g.n_vertices, g.srcs, g.dsts, s0, iters=20,
+                                                     fp64=True)[0]))
+    res = in_threads(*jobs)
+    exact, ppr_err = True, 0.0
+    for i, r in zip(sorted(kept), res):
+        if queries[i][1] == 5:
+            g = gs[queries[i][0]][1]
+            if np.bincount(g.dsts, minlength=g.n_vertices).max() <= 4096:
+                exact &= bool(np.array_equal(kept[i], r[0]))
+            ppr_err = max(ppr_err, pr_error(kept[i], r[1])["rel_l1_vs_fp64"])
+        else:
+            exact &= bool(np.array_equal(kept[i], r))
+    return exact, ppr_err, len(jobs)
+
+
+def c5_sample(queries, gs, per_cell=1, cap_edges=None):
+    """Indices of the first query of every (graph, program) cell."""
+    seen, out = {}, []
+    for i, (k, p, _) in enumerate(queries):
+        if cap_edges is not None and gs[k][1].n_edges > cap_edges:
+            continue
+        if seen.get((k, p), 0) < per_cell:
+            seen[(k, p)] = seen.get((k, p), 0) + 1
+            out.append(i)
+    return out
+
+
+def measure_serve_c5(args, steps, warmup, world, rank, local, with_cpu=True):
     """Serving loop (queries/s, p50/p99) vs one-at-a-time plain runs."""
-    world, rank, local = dist_setup()
     import torch
-    torch.cuda.set_device(local)
     import vertexapi2_gb300 as gas
-    from vertexapi2_gb300._lib import PROGRAM_PPR
-    gas.load()
     stream = torch.cuda.current_stream()
     gs = c5_graphs(set(args.c5_graphs.split(",")) if args.c5_graphs else None)
     srv = gas.GASServer(device=local, lanes=args.c5_lanes)
@@ -822,20 +968,22 @@ def run_serve_c5(args):
     bufs = [(torch.empty(g.n_vertices, dtype=torch.int32).pin_memory().numpy(),
              torch.empty(g.n_vertices, dtype=torch.float32).pin_memory().numpy()) for _, g in gs]
     queries = query_mix(gs, C5_QUERIES, SEED)
-    for w in range(max(args.warmup, 1)):
+    for w in range(max(warmup, 1)):
         serve_pass(srv, ids, gs, queries, float("inf"), bufs, SEED + w)
     barrier(world)
     torch.cuda.synchronize()
     l0 = srv.stats()["kernelLaunches"]
-    steps = []
+    steps_out = []
+    kept = {i: None for i in c5_sample(queries, gs)}
     with ClockSampler(local) as clk:
-        for k in range(args.steps):
-            infos, wall = serve_pass(srv, ids, gs, queries, float("inf"), bufs, SEED + 100 + k)
-            steps.append((serve_summary(infos, gs if k == 0 else None), wall))
+        for k in range(steps):
+            infos, wall = serve_pass(srv, ids, gs, queries, float("inf"), bufs, SEED + 100 + k,
+                                     keep=kept if k == steps - 1 else None)
+            steps_out.append((serve_summary(infos, gs if k == 0 else None), wall))
     launches = srv.stats()["kernelLaunches"] - l0
-    span = allreduce_max(world, float(sum(x["span_s"] for x, _ in steps)))
-    e2e_s = allreduce_max(world, float(sum(w for _, w in steps)))
-    total_q = allreduce_sum(world, float(C5_QUERIES * args.steps))
+    span = allreduce_max(world, float(sum(x["span_s"] for x, _ in steps_out)))
+    e2e_s = allreduce_max(world, float(sum(w for _, w in steps_out)))
+    total_q = allreduce_sum(world, float(C5_QUERIES * steps))
     value = total_q / span
     e2e_value = total_q / e2e_s
     # latency under offered load below capacity
@@ -854,52 +1002,54 @@ def run_serve_c5(args):
     identical, ppr_err = True, 0.0
     alone = {}
     for k, prog, s0, res in singles:
-        out = bufs[k][1 if prog == PROGRAM_PPR else 0]
+        out = bufs[k][1 if prog == 5 else 0]
         _, info = srv.wait(srv.submit(ids[k], prog, s0), out=out)
-        key = f"{gs[k][0]}-{ {1: 'bfs', 2: 'sssp', 5: 'ppr'}[prog] }"
+        key = f"{gs[k][0]}-{PROGRAM_NAMES[prog]}"
         alone.setdefault(key, []).append(((info["doneNs"] - info["submitNs"]) / 1e6, info["rounds"]))
-        if prog == PROGRAM_PPR:
-            a, b = out.astype(np.float64), res.astype(np.float64)
-            ppr_err = max(ppr_err, float(np.abs(a - b).sum() / np.abs(b).sum()))
+        if prog == 5:
+            ppr_err = max(ppr_err, pr_error(out, res)["rel_l1_vs_fp64"])
         else:
             identical &= bool(np.array_equal(out, res))
     st = srv.stats()
     srv.close()
-    cpu = None
-    if rank == 0 and not args.no_cpu:
+    cpu, oracle_parity = None, None
+    if rank == 0 and with_cpu:
+        exact, o_err, n_checked = c5_oracle_check(gs, queries, kept)
+        oracle_parity = {"vs": "oracle on the first query of every (graph, program) cell of the "
+                               "last timed step (served in the full mix)",
+                         "queries": n_checked, "bit_exact_vs_fp32_oracle": exact,
+                         "ppr_max_rel_l1_vs_fp64": o_err, "ok": bool(exact and o_err <= 1e-5)}
         cores = os.cpu_count() or 1
         v, n, wall, kind = cpu_cells(gs, c5_cells(gs), cores)
         cpu = {"value": v, "unit": "queries/s", "cores": cores, "kind": kind,
                "sample": f"one random source per (graph, program) cell, {n} queries on {cores} "
                          f"threads in {wall:.0f} s; value = {cores} / (mix-weighted mean run() "
                          f"time); BFS/SSSP on the {kind} engine, PPR on the restatement"}
-    if rank != 0:
-        return
     d2h = sum(gs[k][1].n_vertices * 4 for k, _, _ in queries)
-    last = steps[-1][0]
-    line = {
+    last = steps_out[-1][0]
+    return {
         "metric": "served queries/s, p50/p99 latency (vs one-at-a-time plain engine)",
-        "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * span / args.steps, "higher_is_better": True,
+        "value": value, "unit": "queries/s", "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": 1e3 * span / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32", "data": "synthetic",
-        "config": {"workload": "serve-c5", "desc": WORKLOADS["serve-c5"]["desc"], "seed": SEED,
-                   "queries_per_step": C5_QUERIES, "lanes": args.c5_lanes, "max_batch": 256,
-                   "graphs": {n: [g.n_vertices, g.n_edges] for n, g in gs},
-                   "arrivals": "timed steps: every query of the step offered at once (capacity); "
-                               "sweep: Poisson at fractions of that capacity",
-                   "l2": "graphs (R-MAT-22: 4.2 M vertices, 126 M edges) and query state larger than L2"},
+        "config": workload_config("serve-c5"),
+        "run": {"queries_per_step": C5_QUERIES, "lanes": args.c5_lanes, "max_batch": 256,
+                "graphs": {n: [g.n_vertices, g.n_edges] for n, g in gs},
+                "arrivals": "timed steps: every query of the step offered at once (capacity); "
+                            "sweep: Poisson at fractions of that capacity",
+                "l2": "graphs (R-MAT-22: 4.2 M vertices, 126 M edges) and query state larger than L2"},
         "latency_ms": {"p50": last["p50_ms"], "p99": last["p99_ms"], "at": "capacity (burst)"},
         "sweep": sweep,
         "mean_batch": last["mean_batch"],
-        "capacity_cells": steps[0][0].get("cells"),
+        "capacity_cells": steps_out[0][0].get("cells"),
         "alone_served_ms": {k: [float(np.mean([a for a, _ in v])), int(v[0][1])]
                             for k, v in sorted(alone.items())},
-        "plain_ms": {f"{gs[k][0]}-{ {1: 'bfs', 2: 'sssp', 5: 'ppr'}[p] }": 1e3 * t
-                     for (k, p), t in sorted(cells.items())},
+        "plain_ms": {f"{gs[k][0]}-{PROGRAM_NAMES[p]}": 1e3 * t for (k, p), t in sorted(cells.items())},
         "one_at_a_time": {"value": single_qps, "unit": "queries/s",
                           "sample_queries": len(singles), "speedup": value / single_qps,
                           "results_identical_bfs_sssp": identical,
                           "ppr_max_rel_l1_vs_plain": ppr_err},
+        "parity": oracle_parity,
         "server": {"batches": st["batches"], "memory_waits": st["memoryWaits"],
                    "peak_bytes": st["peakBytesInUse"]},
         "cpu_baseline": cpu,
@@ -908,7 +1058,47 @@ def run_serve_c5(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line))
+
+
+def per_algo_entry(line: dict) -> dict:
+    """The per_algo summary of a workload's line."""
+    keep = ("value", "unit", "steps", "warmup", "ms_per_step", "dtype", "config", "run", "roofline",
+            "cpu_baseline", "parity", "e2e", "gpu_launches", "clocks", "one_at_a_time", "per_set",
+            "latency_ms", "sweep", "mean_batch", "plain_ms", "alone_served_ms", "server")
+    return {k: line[k] for k in keep if k in line}
+
+
+def run_ours(args):
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    import vertexapi2_gb300 as gas
+    gas.load()
+    if not gas.device_supported(local):
+        raise SystemExit(f"cuda:{local} is not an sm_103 device")
+    with_cpu = not args.no_cpu
+
+    def measure(name, steps, warmup):
+        if name == "batch-c4":
+            return measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu)
+        if name == "serve-c5":
+            return measure_serve_c5(args, steps, warmup, world, rank, local, with_cpu)
+        return measure_plain(name, steps, warmup, world, rank, local, with_cpu)
+
+    line = measure(args.workload, args.steps, args.warmup)
+    if args.workload == HEADLINE and world == 1 and not args.no_per_algo:
+        per = {}
+        for name in PER_ALGO:
+            t0 = time.perf_counter()
+            per[name] = per_algo_entry(measure(name, args.steps, args.warmup))
+            per[name]["bench_wall_s"] = time.perf_counter() - t0
+        line["per_algo"] = per
+        line["gpu_launches"] += sum(int(x.get("gpu_launches") or 0) for x in per.values())
+        line["gpu_launches_note"] = ("headline steps plus every per_algo workload's timed "
+                                     "steps (each entry lists its own)")
+    if rank == 0:
+        line["native_libraries"] = mapped_libraries()
+        print(json.dumps(line))
 
 
 def main():
@@ -917,8 +1107,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sssp-grid1024")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=HEADLINE)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline and oracle legs")
+    ap.add_argument("--no-per-algo", action="store_true",
+                    help="headline workload only (no per_algo block)")
     ap.add_argument("--rmat-scale", type=int, default=None,
                     help="smaller R-MAT scale for the R-MAT workloads (profiling captures)")
     ap.add_argument("--grid-side", type=int, default=1024,
@@ -939,10 +1131,6 @@ def main():
             RMAT_SCALE[k] = args.rmat_scale
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "batch-c4":
-        run_batch_c4(args)
-    elif args.workload == "serve-c5":
-        run_serve_c5(args)
     else:
         run_ours(args)
 

@@ -30,6 +30,11 @@ class OraStats(C.Structure):
                 ("run_ns", C.c_int64)]
 
 
+class OraGraph(C.Structure):
+    _fields_ = [("nVertices", C.c_int32), ("nEdges", C.c_int64), ("srcs", C.POINTER(C.c_int32)),
+                ("dsts", C.POINTER(C.c_int32)), ("weights", C.POINTER(C.c_int32))]
+
+
 _PI = C.POINTER(C.c_int32)
 _PS = C.POINTER(OraStats)
 _SIGS = {
@@ -60,6 +65,15 @@ class Engine:
                 continue
             fn.restype = C.c_int
             fn.argtypes = args
+        if prefix == "ora_":
+            self.lib.ora_gen_rmat.restype = C.c_int
+            self.lib.ora_gen_rmat.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                              C.c_double, C.c_uint64, C.c_int32, C.c_int32,
+                                              C.c_int32, C.POINTER(OraGraph)]
+            self.lib.ora_gen_grid.restype = C.c_int
+            self.lib.ora_gen_grid.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_uint64,
+                                              C.c_int32, C.c_int32, C.POINTER(OraGraph)]
+            self.lib.ora_graph_free.argtypes = [C.POINTER(OraGraph)]
         if prefix == "ref_":
             self.lib.ref_load_graph.restype = C.c_int
             self.lib.ref_load_graph.argtypes = [C.c_char_p, _PI, _PI, C.POINTER(_PI),
@@ -150,6 +164,32 @@ class Engine:
         st = self._call("run_ppr_f64" if fp64 else "run_ppr_f32", n, len(s), ps, pd, source, a,
                         iters, out.ctypes.data_as(C.POINTER(ct)), cap=stats_cap)
         return out[:n], st
+
+    def _take_graph(self, g: OraGraph):
+        m = int(g.nEdges)
+        take = lambda p: np.ctypeslib.as_array(p, shape=(max(m, 1),))[:m].copy()
+        out = (int(g.nVertices), take(g.srcs), take(g.dsts), take(g.weights) if g.weights else None)
+        self.lib.ora_graph_free(C.byref(g))
+        return out
+
+    def gen_rmat(self, scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1,
+                 symmetrize=False, weights=None):
+        """The benchmark's seeded R-MAT graph (restatement only):
+        (n_vertices, srcs, dsts, weights or None)."""
+        g = OraGraph()
+        lo, hi = weights if weights else (0, -1)
+        if self.lib.ora_gen_rmat(scale, edge_factor, a, b, c, seed, int(symmetrize), lo, hi,
+                                 C.byref(g)) != 0:
+            raise ValueError("ora_gen_rmat rejected its arguments")
+        return self._take_graph(g)
+
+    def gen_grid(self, rows, cols, p_delete=0.15, seed=1, weights=(1, 100)):
+        """The benchmark's seeded lattice (restatement only)."""
+        g = OraGraph()
+        lo, hi = weights if weights else (0, -1)
+        if self.lib.ora_gen_grid(rows, cols, p_delete, seed, lo, hi, C.byref(g)) != 0:
+            raise ValueError("ora_gen_grid rejected its arguments")
+        return self._take_graph(g)
 
     def load_graph(self, path: str):
         """graphio.cpp loadGraph (reference engine only)."""

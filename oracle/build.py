@@ -8,8 +8,8 @@ Two libraries, both outside the product:
 * ``oracle/_ref/libgas_ref.so`` -- the reference's own CPU engine
   (refgas.h, util.h, graphio.cpp) compiled in place from the reference
   tree by g++ with ref_harness.cpp.  Only built where that tree exists
-  (``GAS_REF_DIR``, default ``/root/reference``); it pins the restatement
-  and produces the golden vectors under tests/golden/.
+  (see ``ref_dir``); it pins the restatement and produces the golden
+  vectors under tests/golden/.
 
 Run ``python oracle/build.py`` to build both (the second only when the
 reference tree is present).
@@ -27,8 +27,20 @@ PORT_LIB = os.path.join(BUILD_DIR, "libgas_oracle.so")
 REF_LIB = os.path.join(REF_OUT_DIR, "libgas_ref.so")
 
 
+REPO = os.path.dirname(HERE)
+# Where this recipe looks for the reference source tree, in order: the
+# GAS_REF_DIR override, an installed copy under baseline/_ref, and the
+# read-only checkout that the development container mounts.
+REF_DIR_CANDIDATES = (os.path.join(REPO, "baseline", "_ref"), "/root/reference")
+
+
 def ref_dir() -> str:
-    return os.environ.get("GAS_REF_DIR", "/root/reference")
+    if os.environ.get("GAS_REF_DIR"):
+        return os.environ["GAS_REF_DIR"]
+    for d in REF_DIR_CANDIDATES:
+        if os.path.exists(os.path.join(d, "refgas.h")):
+            return d
+    return REF_DIR_CANDIDATES[0]
 
 
 def _newer(target: str, sources: list[str]) -> bool:
@@ -39,13 +51,14 @@ def _newer(target: str, sources: list[str]) -> bool:
 
 
 def build_port(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("gas_oracle.c", "gas_oracle.h", "gas_oracle_engine.inc")]
+    srcs = [os.path.join(HERE, f) for f in ("gas_oracle.c", "gas_oracle_gen.c", "gas_oracle.h",
+                                            "gas_oracle_engine.inc")]
     if not force and _newer(PORT_LIB, srcs):
         return PORT_LIB
     os.makedirs(BUILD_DIR, exist_ok=True)
     # -ffp-contract=off: identical FP32 results on x86-64 and aarch64
-    cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off",
-           "-o", PORT_LIB, srcs[0], "-lm"]
+    cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
+           "-o", PORT_LIB, srcs[0], srcs[1], "-lm"]
     subprocess.run(cmd, check=True)
     return PORT_LIB
 

@@ -94,6 +94,22 @@ int ora_run_ppr_f64(int32_t nV, int32_t nE, const int32_t *srcs,
                     const int32_t *dsts, int32_t source, double alpha,
                     int32_t iters, double *rank, ora_stats *stats);
 
+/* Seeded synthetic graphs (gas_oracle_gen.c): an implementation of the
+ * benchmark's R-MAT and lattice generators independent of the product
+ * library, so that CPU-only measurements never load it.  Outputs are
+ * malloc'd; release them with ora_graph_free.  Return 0 on success. */
+typedef struct {
+  int32_t nVertices;
+  int64_t nEdges;
+  int32_t *srcs, *dsts, *weights; /* weights NULL when none were asked for */
+} ora_graph;
+
+int ora_gen_rmat(int32_t scale, int32_t edgeFactor, double a, double b, double c,
+                 uint64_t seed, int32_t symmetrize, int32_t wLo, int32_t wHi, ora_graph *out);
+int ora_gen_grid(int32_t rows, int32_t cols, double pDelete, uint64_t seed, int32_t wLo,
+                 int32_t wHi, ora_graph *out);
+void ora_graph_free(ora_graph *g);
+
 #ifdef __cplusplus
 }
 #endif

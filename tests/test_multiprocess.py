@@ -58,3 +58,10 @@ def test_reference_arm_on_two_ranks_prints_one_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0
+    # the reference arm builds its graphs with the oracle's generators and
+    # never maps the product library
+    assert not any("libgas_gb300" in p for p in d["native_libraries"]), d["native_libraries"]
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.workload_config("bfs-rmat16", bench.make_workload(
+        "bfs-rmat16", source="oracle")["g"])

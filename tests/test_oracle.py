@@ -119,3 +119,49 @@ def test_scatter_program_port_matches_reference():
         for x, y in zip(a[:3], b[:3]):
             assert np.array_equal(x, y)
         assert a[1].sum() > 0
+
+
+# The oracle's generators (gas_oracle_gen.c) are a second implementation of
+# the benchmark graphs, used where the product library must not be loaded.
+GEN_CASES = {
+    "rmat8_sym": ("rmat", dict(scale=8, seed=11, symmetrize=True, weights=(1, 255))),
+    "rmat10_dir": ("rmat", dict(scale=10, seed=12, symmetrize=False, weights=(1, 100))),
+    "grid16": ("grid", (16, 16, 0.15, 13)),
+    "grid40x30": ("grid", (40, 30, 0.15, 14)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(GEN_CASES))
+def test_oracle_generators_match_golden_hashes(port, name):
+    import hashlib
+    import json
+    import os
+    from conftest import GOLDEN
+    idx = json.load(open(os.path.join(GOLDEN, "index.json")))["graphs"][name]
+    kind, args = GEN_CASES[name]
+    nv, s, d, w = port.gen_rmat(**args) if kind == "rmat" else port.gen_grid(*args)
+    assert nv == idx["n_vertices"] and len(s) == idx["n_edges"]
+    h = hashlib.sha256()  # tests/golden/make_golden.py edge_hash
+    for a in (s, d, w):
+        h.update(np.ascontiguousarray(a, dtype="<i4").tobytes())
+    assert h.hexdigest() == idx["edge_sha256"]
+
+
+@pytest.mark.parametrize("kind,args", [
+    ("rmat", dict(scale=16, seed=1, symmetrize=True)),             # BFS benchmark graph
+    ("rmat", dict(scale=14, seed=15, symmetrize=True, weights=(1, 255))),
+    ("rmat", dict(scale=12, seed=3, symmetrize=False)),
+    ("grid", (1024, 1024, 0.15, 1)),                                # SSSP benchmark graph
+    ("grid", (7, 300, 0.5, 9)),
+])
+def test_oracle_generators_match_product(port, gas_lib, kind, args):
+    from vertexapi2_gb300 import graphs
+    if kind == "rmat":
+        nv, s, d, w = port.gen_rmat(**args)
+        g = graphs.rmat(**args)
+    else:
+        nv, s, d, w = port.gen_grid(*args)
+        g = graphs.grid(*args)
+    assert nv == g.n_vertices
+    assert np.array_equal(s, g.srcs) and np.array_equal(d, g.dsts)
+    assert (w is None and g.weights is None) or np.array_equal(w, g.weights)
