@@ -173,16 +173,20 @@ GAS_API gas_status gas_engine_set_fused_rounds(gas_engine *e, int32_t on);
  * in device memory the caller owns: outOffsets[nVertices+1] and
  * outDests[nEdges] (CSR), depth[nVertices] (written: -1 unreached, else the
  * round at which the vertex was reached, as bfs.cu:31-78).  All scratch is
- * one fixed file-scope __device__ array (about 3.4 MB, held by every GPU
- * that loads the library until exit), so graphs are limited to
- * GAS_NOALLOC_MAX_VERTICES vertices and GAS_NOALLOC_MAX_EDGES edges; larger
- * ones are rejected with GAS_ERR_INVALID.  The first call on a device looks
- * up that array's device address, so make it before any stream capture.
- * Every call reuses the same array: calls that overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller.
- * Runs on `stream` (a cudaStream_t, NULL = legacy default stream) and
- * returns when the search is done; *rounds (may be NULL) receives the
- * number of rounds. */
+ * one fixed file-scope __device__ array (about 3.4 MB), so graphs are
+ * limited to GAS_NOALLOC_MAX_VERTICES vertices and GAS_NOALLOC_MAX_EDGES
+ * edges; larger ones are rejected with GAS_ERR_INVALID.  A GPU holds the
+ * array from the time the library's device code is loaded on it until the
+ * process exits; under CUDA's default lazy loading that is the first call
+ * on the device, which can therefore fail with an out-of-memory status when
+ * another allocator has already taken the free memory.  That first call on
+ * a device also looks up the array's device address (kept for the process's
+ * life: calls after a cudaDeviceReset are not supported), so make it before
+ * any stream capture.  Every call reuses the same array: calls that overlap
+ * on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Runs on `stream` (a cudaStream_t, NULL =
+ * legacy default stream) and blocks until the search is done; *rounds (may
+ * be NULL) receives the number of rounds. */
 #define GAS_NOALLOC_MAX_VERTICES 65536
 #define GAS_NOALLOC_MAX_EDGES 2097152
 GAS_API gas_status gas_bfs_noalloc(int32_t nVertices, int32_t nEdges, const int32_t *outOffsets,

@@ -7,8 +7,12 @@
 // entry point serves them: the caller passes the graph and the output in
 // device memory it already owns, and every scratch buffer the search needs
 // (frontier and scatter lists, merge-path splits, activation stamps,
-// control words) lives in one file-scope __device__ array of fixed size,
-// which every GPU that loads this library holds until the process exits.
+// control words) lives in one file-scope __device__ array of fixed size.
+// A GPU holds that array from the moment this library's device code is
+// loaded on it until the process exits.  With CUDA's lazy module loading
+// (the default) that moment is the first call on the device, so a caller
+// whose allocator has already claimed the free device memory can see that
+// first call fail with an out-of-memory status; later calls cannot.
 //
 // The search is the BFS vertex program (bfs.cu:31-78) run to completion by
 // the same persistent kernel as gas_engine_run.
@@ -71,7 +75,9 @@ __global__ void fill_minus_one(int32_t *p, int32_t n) {
 }
 
 // Once per device, with that device current: the scratch's device address
-// and the co-resident grid of the persistent kernel.
+// and the co-resident grid of the persistent kernel.  Both are kept for the
+// life of the process; a cudaDeviceReset (which unloads the module and may
+// move the array) is not supported between calls.
 gas_status setup(int dev, unsigned char **scratch, int *grid) {
   std::lock_guard<std::mutex> lock(g_mu);
   if (!g_scratch[dev]) {
@@ -127,6 +133,13 @@ gas_status gas_bfs_noalloc(int32_t nVertices, int32_t nEdges, const int32_t *out
     e = cudaMemsetAsync(sc + kOffMark, 0, sizeof(int32_t) * (size_t)nVertices, s);
   if (e != cudaSuccess) return cuda_fail(e, "no-alloc scratch reset");
   fill_minus_one<<<(nVertices + 255) / 256, 256, 0, s>>>(depth, nVertices);  // bfs.cu:143-145
+  // The first round's frontier is the range [source, source + 1): its edge
+  // positions are counted from outOffsets[source], as gas_engine_run counts
+  // them from the CSC offset of the range start.
+  int32_t base = 0;
+  e = cudaMemcpyAsync(&base, outOffsets + source, sizeof(base), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "no-alloc BFS range offset");
 
   gas_run_args ra;
   memset(&ra, 0, sizeof(ra));
@@ -141,6 +154,7 @@ gas_status gas_bfs_noalloc(int32_t nVertices, int32_t nEdges, const int32_t *out
   a.rangeMode = 1;
   a.rangeStart = source;
   a.rangeCount = 1;
+  a.rangeBase = base;
   a.capacity = nVertices;
   a.maxScatTiles = kMaxTiles;
   a.carryVal = tail->carryVal;
