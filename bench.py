@@ -663,7 +663,9 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
 # ------------------------------------------------------------------- C4 --
 def measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu=True):
     """Batched multi-source queries (queries/s) vs one-at-a-time plain runs,
-    with a sample of every set checked against the oracle."""
+    with a sample of every set checked against the oracle.  value counts
+    the 256 BFS + 256 SSSP queries per graph; a batched personalised
+    PageRank set (256 sources on the R-MAT graph) is reported beside it."""
     import torch
     import vertexapi2_gb300 as gas
     stream = torch.cuda.current_stream()
@@ -671,98 +673,115 @@ def measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu=True):
     nq = 256
     gs = c4_graphs(args.rmat_scale or 21, args.grid_side)
     only = set(args.c4_sets.split(",")) if args.c4_sets else None
-    sets, batches = [], []
+    sets = []
+    progs = {gs[0][0]: (1, 2, 5), gs[1][0]: (1, 2)}
     for name, g in gs:
-        b = gas.GASBatch(device=local, stream=stream.cuda_stream)
-        b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
-        batches.append(b)
-        for prog in (1, 2):
+        for prog in progs[name]:
             src = rng.integers(0, g.n_vertices, nq).astype(np.int32)
             key = f"{name}-{PROGRAM_NAMES[prog]}"
             if only is not None and key not in only:
                 continue
+            # one batch object per set: its tuned settings and captured
+            # CUDA graph stay in place from step to step
+            b = gas.GASBatch(device=local, stream=stream.cuda_stream)
+            b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights if prog == 2 else None)
             if args.no_autotune:
-                cfg = (256, 0, args.c4_delta if prog == 2 else 0)
+                b.set_config(256, 0, True)
+                b.set_delta(args.c4_delta if prog == 2 else 0)
             else:
-                cfg = b.autotune(prog, nq) + (b.get_delta() if prog == 2 else 0,)
-            sets.append((key, g, b, prog, src, cfg))
+                b.autotune(prog, nq)
+            sets.append((key, g, b, prog, src, b.tuning()))
     per_set_ms = [0.0] * len(sets)
     per_set_rounds = [0] * len(sets)
 
     def batched_step():
-        ms = 0.0
-        for i, (key, g, b, prog, src, cfg) in enumerate(sets):
-            b.set_config(cfg[0], cfg[1], True)
-            b.set_delta(cfg[2])
+        for i, (key, g, b, prog, src, t) in enumerate(sets):
             _, per_set_rounds[i] = b.run(prog, src, want_results=False)
-            ms += b.last_ms()
             per_set_ms[i] += b.last_ms()
-        return ms
     for _ in range(warmup):
         batched_step()
     barrier(world)
     torch.cuda.synchronize()
     per_set_ms[:] = [0.0] * len(sets)
     with ClockSampler(local) as clk:
-        step_ms = [batched_step() for _ in range(steps)]
-    total_ms = allreduce_max(world, float(sum(step_ms)))
-    queries = allreduce_sum(world, float(len(sets) * nq * steps))
+        for _ in range(steps):
+            batched_step()
+    head = [i for i, x in enumerate(sets) if x[3] != 5]   # BFS + SSSP: the metric's queries
+    total_ms = allreduce_max(world, float(sum(per_set_ms[i] for i in head)))
+    queries = allreduce_sum(world, float(len(head) * nq * steps))
     value = queries / (total_ms / 1e3)
     # end to end: sources up and every query's result copied to host memory
-    t0 = time.perf_counter()
-    outs = []
-    for key, g, b, prog, src, cfg in sets:
-        b.set_config(cfg[0], cfg[1], True)
-        b.set_delta(cfg[2])
-        outs.append(b.run(prog, src, want_results=True)[0])
-    e2e_s = time.perf_counter() - t0
-    e2e_value = len(sets) * nq / e2e_s
-    d2h = sum(nq * g.n_vertices * 4 for _, g, _, _, _, _ in sets)
+    outs = [None] * len(sets)
+    e2e_s = 0.0
+    for i, (key, g, b, prog, src, t) in enumerate(sets):
+        t0 = time.perf_counter()
+        outs[i] = b.run(prog, src, want_results=True)[0]
+        if i in head:
+            e2e_s += time.perf_counter() - t0
+    e2e_value = len(head) * nq / e2e_s
+    d2h = sum(nq * sets[i][1].n_vertices * 4 for i in head)
     # one-at-a-time plain engine on a sample of the same queries
+    from vertexapi2_gb300 import programs as P
     sample = 8
     single_ms, single_n = 0.0, 0
-    parity = True
+    parity, ppr_plain_err = True, 0.0
     per_set = {}
-    for i, (key, g, b, prog, src, cfg) in enumerate(sets):
-        s_ms0 = single_ms
+    for i, (key, g, b, prog, src, t) in enumerate(sets):
+        s_ms = 0.0
         e = gas.GASEngine(prog, device=local, stream=stream.cuda_stream)
         for q, s0 in enumerate(src[:sample]):
+            s0 = int(s0)
             if prog == 1:
-                vd = np.full(g.n_vertices, -1, np.int32)
+                vd, act = P.bfs_init(g.n_vertices), (s0, s0 + 1)
+            elif prog == 2:
+                vd, act = P.sssp_init(g.n_vertices, s0), (0, g.n_vertices)
             else:
-                vd = np.full(g.n_vertices, 2**31 - 1 - 100000, np.int32)
-                vd[int(s0)] = 0
+                vd, act = P.ppr_init(g.n_vertices, g.srcs, s0), (0, g.n_vertices)
             e.set_graph(g.n_vertices, vd, g.srcs, g.dsts, g.weights if prog == 2 else None) \
                 if q == 0 else e.set_vertex_data(vd)
-            act = (int(s0), int(s0) + 1) if prog == 1 else (0, g.n_vertices)
             e.set_active(*act)
-            e.run()
-            single_ms += e.last_run_ms()
-            single_n += 1
+            e.run(20 if prog == 5 else 0)
+            s_ms += e.last_run_ms()
             e.get_results()  # into the array borrowed by set_graph
-            parity &= bool(np.array_equal(e.vertex_data, outs[i][q]))
+            if prog == 5:
+                ppr_plain_err = max(ppr_plain_err, pr_error(outs[i][q], e.vertex_data["rank"])["rel_l1_vs_fp64"])
+            else:
+                parity &= bool(np.array_equal(e.vertex_data, outs[i][q]))
         e.close()
+        if i in head:
+            single_ms += s_ms
+            single_n += sample
         per_set[key] = {"batched_ms_per_256": per_set_ms[i] / steps,
                         "batched_rounds": per_set_rounds[i],
-                        "single_ms": (single_ms - s_ms0) / sample,
-                        "speedup": ((single_ms - s_ms0) / sample * nq) / (per_set_ms[i] / steps)}
-    for b in batches:
-        b.close()
+                        "single_ms": s_ms / sample,
+                        "speedup": (s_ms / sample * nq) / (per_set_ms[i] / steps),
+                        "tuning": t}
+    for x in sets:
+        x[2].close()
     single_qps = single_n / (single_ms / 1e3)
     # oracle parity on a sample of every set (two queries per set, at once)
-    oracle_ok, oracle_n, cpu = None, 0, None
+    oracle_ok, oracle_n, ppr_err, cpu = None, 0, 0.0, None
     if rank == 0 and with_cpu:
         import oracle
         port = oracle.port()
         jobs = []
-        for i, (key, g, b, prog, src, cfg) in enumerate(sets):
+        for i, (key, g, b, prog, src, t) in enumerate(sets):
             for q in (0, nq - 1):
+                x = int(src[q])
                 if prog == 1:
-                    jobs.append((i, q, lambda g=g, s0=int(src[q]): port.bfs(g.n_vertices, g.srcs, g.dsts, s0)[0]))
+                    f = lambda g=g, x=x: port.bfs(g.n_vertices, g.srcs, g.dsts, x)[0]
+                elif prog == 2:
+                    f = lambda g=g, x=x: port.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, x)[0]
                 else:
-                    jobs.append((i, q, lambda g=g, s0=int(src[q]): port.sssp(g.n_vertices, g.srcs, g.dsts, g.weights, s0)[0]))
+                    f = lambda g=g, x=x: port.ppr(g.n_vertices, g.srcs, g.dsts, x, iters=20, fp64=True)[0]
+                jobs.append((i, q, f))
         res = in_threads(*[f for _, _, f in jobs])
-        oracle_ok = all(np.array_equal(r, outs[i][q]) for (i, q, _), r in zip(jobs, res))
+        oracle_ok = True
+        for (i, q, _), r in zip(jobs, res):
+            if sets[i][3] == 5:
+                ppr_err = max(ppr_err, pr_error(outs[i][q], r)["rel_l1_vs_fp64"])
+            else:
+                oracle_ok &= bool(np.array_equal(r, outs[i][q]))
         oracle_n = len(jobs)
         cores = os.cpu_count() or 1
         cells = c4_cells(gs)
@@ -777,17 +796,20 @@ def measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu=True):
         "ms_per_step": total_ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": workload_config("batch-c4"),
-        "run": {"queries_per_step": len(sets) * nq,
-                "autotuned": {k: list(c) for k, _, _, _, _, c in sets},
-                "l2": "inputs (R-MAT-21 CSC/CSR, 2 GB query state) larger than L2"},
+        "run": {"queries_per_step": len(head) * nq,
+                "l2": "inputs (R-MAT-21 CSC/CSR, 2 GB query state) larger than L2",
+                "sets": "one persistent launch per set of 256 queries (BFS and SSSP launched "
+                        "separately), each replayed from its captured CUDA graph"},
         "one_at_a_time": {"value": single_qps, "unit": "queries/s", "sample_queries": single_n,
-                          "speedup": value / single_qps, "results_identical": parity},
+                          "speedup": value / single_qps, "results_identical": parity,
+                          "ppr_max_rel_l1_vs_plain": ppr_plain_err},
         "per_set": per_set,
-        "parity": {"vs": "oracle BFS/SSSP on the first and last source of every set",
-                   "queries": oracle_n, "bit_exact": oracle_ok,
-                   "ok": bool(oracle_ok and parity) if oracle_ok is not None else None},
+        "parity": {"vs": "oracle BFS/SSSP (bit-exact) and FP64 PPR on the first and last source "
+                         "of every set", "queries": oracle_n, "bit_exact": oracle_ok,
+                   "ppr_max_rel_l1_vs_fp64": ppr_err,
+                   "ok": bool(oracle_ok and parity and ppr_err <= 1e-5) if oracle_ok is not None else None},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * nq * len(sets),
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": 4 * nq * len(head),
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": 5 * len(sets) * steps,
         "clocks": clk.summary(),

@@ -194,11 +194,14 @@ GAS_API gas_status gas_bfs_noalloc(int32_t nVertices, int32_t nEdges, const int3
                                    void *stream, int32_t *rounds);
 
 /* ---------------- batched multi-source queries --------------------------- */
-/* Many BFS or SSSP queries with their own sources on one resident graph
- * (no counterpart in the reference, which runs one source per engine).
- * Each group of up to 256 queries is one persistent launch, captured once
- * per shape into a CUDA graph and replayed; every query's result equals its
- * single-source gas_engine_run result bit for bit. */
+/* Many BFS, SSSP or personalised PageRank queries with their own sources on
+ * one resident graph (no counterpart in the reference, which runs one
+ * source per engine).  Each group of up to 256 queries is one persistent
+ * launch, captured once per shape into a CUDA graph and replayed; every BFS
+ * or SSSP query's result equals its single-source gas_engine_run result bit
+ * for bit, and every PPR query's ranks equal the served PPR query's (the
+ * same sums in the same order: a left fold in CSC order for vertices of
+ * in-degree <= 4096, bit for bit the FP32 oracle's). */
 typedef struct gas_batch_s gas_batch;
 
 GAS_API gas_status gas_batch_create(int32_t device, void *stream, gas_batch **out);
@@ -208,21 +211,33 @@ GAS_API gas_status gas_batch_destroy(gas_batch *b);
 GAS_API gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
                                        const int32_t *srcs, const int32_t *dsts,
                                        const int32_t *weights);
-/* program = GAS_PROGRAM_BFS or GAS_PROGRAM_SSSP.  results (may be NULL) is a
- * host array of nQueries * nVertices int32, query-major: BFS depth (-1 =
- * unreached) or SSSP distance (2147383647 = unreached, sssp.cu:32-33).
- * *rounds receives the largest round count of the batches. */
+/* program = GAS_PROGRAM_BFS, GAS_PROGRAM_SSSP or GAS_PROGRAM_PPR (alpha
+ * 0.15, teleport to the source, 20 rounds, every vertex active at the
+ * start as the serving loop runs it).  results (may be NULL) is a host
+ * array of nQueries * nVertices 4-byte values, query-major: BFS depth
+ * (int32, -1 = unreached), SSSP distance (int32, 2147383647 = unreached,
+ * sssp.cu:32-33) or PPR rank (float32).  *rounds receives the largest round
+ * count of the batches. */
 GAS_API gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries,
                                  const int32_t *sources, int32_t *results, int32_t *rounds);
 /* Work units of at most chunkEdges in-edges, CTAs per SM (0 = as many as
  * fit), CUDA-graph replay on/off.  Results do not depend on them. */
 GAS_API gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocksPerSM,
                                         int32_t useGraphs);
-/* Times the candidate configurations on nQueries random sources and keeps
- * the fastest; reports the chosen chunk size and CTAs per SM (for SSSP it
- * first chooses the bucket width, see gas_batch_set_delta). */
+/* Times candidate configurations on nQueries random sources and keeps the
+ * fastest, one setting at a time: for SSSP the bucket width
+ * (gas_batch_set_delta); for BFS and SSSP the frontier form
+ * (gas_batch_set_frontier, where pairs are allowed) and, for vertex-mask
+ * frontiers, the push/pull switch alpha (gas_batch_set_policy); then the
+ * work-unit chunk (edges per warp unit, i.e. warps per high-degree vertex)
+ * and CTAs per SM (PPR: CTAs per SM only).  Reports the chosen chunk size
+ * and CTAs per SM; gas_batch_get_tuning reads every setting. */
 GAS_API gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
                                       int32_t *chunkEdges, int32_t *blocksPerSM);
+/* The current settings: chunk edges, CTAs per SM, alpha, frontier form,
+ * SSSP bucket width (any pointer may be NULL). */
+GAS_API gas_status gas_batch_get_tuning(gas_batch *b, int32_t *chunkEdges, int32_t *blocksPerSM,
+                                        int32_t *alpha, int32_t *frontier, int32_t *delta);
 /* Round policy: a round pushes from the vertices that changed last round
  * when their out-degree total times alpha is at most nEdges, otherwise it
  * pulls over every vertex (default alpha 10; 0 = always push).  Results do

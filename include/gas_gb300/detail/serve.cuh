@@ -162,6 +162,26 @@ struct PprArgs {
   float teleport;             // alpha
 };
 
+// The graph part of PprArgs, from a graph's PPR arrays (the work-unit block
+// `mem` holds unitV | unitBeg | unitLen | unitSlot | slotFirst | slotCount |
+// slotHub, `units` and `slots` entries long).
+inline void ppr_args_graph(PprArgs &a, const int32_t *inSources, const int32_t *outDegree,
+                           const uint8_t *lastActive, const int32_t *mem, int32_t units,
+                           int32_t slots) {
+  const size_t nu = (size_t)(units > 0 ? units : 1), ns = (size_t)(slots > 0 ? slots : 1);
+  a.inSources = inSources;
+  a.outDegree = outDegree;
+  a.lastActive = lastActive;
+  a.nUnits = units;
+  a.unitV = mem;
+  a.unitBeg = a.unitV + nu;
+  a.unitLen = a.unitBeg + nu;
+  a.unitSlot = a.unitLen + nu;
+  a.slotFirst = a.unitSlot + nu;
+  a.slotCount = a.slotFirst + ns;
+  a.slotHub = a.slotCount + ns;
+}
+
 __device__ __forceinline__ float ppr_contrib(float rank, int deg) {
   return deg > 0 ? __fdiv_rn(rank, (float)deg) : 0.0f;
 }
@@ -229,7 +249,7 @@ __global__ void ppr_sources_kernel(const PprArgs a) {
 // lane, coalesced), issues the D gathered rows' loads, then each lane folds
 // its queries' D values in edge order.
 template <int QP>
-__global__ void __launch_bounds__(256) ppr_round_kernel(const PprArgs a, int r) {
+__device__ __forceinline__ void ppr_round(const PprArgs &a, int r) {
   using S = PprShape<QP>;
   constexpr int L = S::L, G = S::G, W = S::W, D = S::D, M = S::M;
   const int lane = threadIdx.x & 31;
@@ -317,6 +337,25 @@ __global__ void __launch_bounds__(256) ppr_round_kernel(const PprArgs a, int r) 
       }
     }
   }
+}
+
+template <int QP>
+__global__ void __launch_bounds__(256) ppr_round_kernel(const PprArgs a, int r) {
+  ppr_round<QP>(a, r);
+}
+
+// Every round of a PPR batch in one cooperative launch (the batched engine,
+// gas_batch_run): the served round body, rounds separated by bounded grid
+// barriers.  *roundsOut receives the rounds completed.
+template <int QP>
+__global__ void __launch_bounds__(256) ppr_run_kernel(const PprArgs a, int rounds, unsigned *barrier,
+                                                      unsigned *errWord, int32_t *roundsOut) {
+  int r = 0;
+  for (; r < rounds; ++r) {
+    ppr_round<QP>(a, r);
+    if (!grid_barrier(barrier, errWord)) break;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *roundsOut = r;
 }
 
 }  // namespace detail

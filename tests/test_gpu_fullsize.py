@@ -13,7 +13,8 @@ benchmark configuration is checked here at its full size:
   frontier counts equal to the oracle's;
 * batched queries: 256 BFS + 256 SSSP sources on R-MAT-21 symmetrised
   (w in [1,255]) and on the 1024x1024 lattice, a fixed sample of every set
-  bit-exact against single-source oracle runs;
+  bit-exact against single-source oracle runs, and 256 personalised
+  PageRank sources within 1e-5 of the FP64 oracle;
 * serving: the 8-graph mix offered at once, one query of every (graph,
   program) cell checked against the oracle.
 
@@ -119,6 +120,16 @@ def test_c4_batched_sets_vs_oracle(gpu, port, graph):
                                    for q in sample])
             for q, ref in zip(sample, refs):
                 assert np.array_equal(got[q], ref), f"{graph} program {prog} query {q}"
+        # personalised PageRank batched the same way (256 sources, 20 rounds)
+        sources = rng.integers(0, g.n_vertices, 256).astype(np.int32)
+        b.autotune(PROGRAM_PPR, 256)
+        got, rounds = b.run(PROGRAM_PPR, sources)
+        assert rounds == 20
+        refs = in_threads([lambda x=int(sources[q]): port.ppr(g.n_vertices, g.srcs, g.dsts, x,
+                                                               iters=20, fp64=True)[0]
+                           for q in sample[:4]])
+        for q, ref in zip(sample[:4], refs):
+            assert rel_l1(got[q], ref) <= PR_REL_L1, f"{graph} PPR query {q}"
 
 
 def test_c5_serving_eight_graphs_vs_oracle(gpu, port):

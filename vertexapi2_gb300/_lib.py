@@ -98,6 +98,7 @@ SIGNATURES = {
     "gas_batch_set_delta": (_I32, [_P, _I32]),
     "gas_batch_set_frontier": (_I32, [_P, _I32]),
     "gas_batch_get_delta": (_I32, [_P, _PI32]),
+    "gas_batch_get_tuning": (_I32, [_P, _PI32, _PI32, _PI32, _PI32, _PI32]),
     # serving loop
     "gas_server_create": (_I32, [_I32, C.POINTER(ServerConfig), C.POINTER(_P)]),
     "gas_server_destroy": (_I32, [_P]),

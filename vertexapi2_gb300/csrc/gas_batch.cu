@@ -1,12 +1,14 @@
-// Batched multi-source BFS / SSSP (gas_batch_* in gas_gb300.h).
+// Batched multi-source BFS / SSSP / personalised PageRank (gas_batch_* in
+// gas_gb300.h).
 //
 // Many queries with their own sources on one resident graph: each batch of
 // up to 256 queries is one persistent cooperative launch (kernels in
-// gas_gb300/detail/batch.cuh), and the whole batch -- source upload, state
+// gas_gb300/detail/batch.cuh; PPR's round body is the serving loop's, in
+// gas_gb300/detail/serve.cuh), and the whole batch -- source upload, state
 // reset, the run and the query-major transpose of the results -- is
 // captured once per shape into a CUDA graph and replayed.  Work units (a
-// vertex's in-edges, hubs split into chunks) and the launch shape are
-// chosen by gas_batch_autotune.
+// vertex's in-edges, hubs split into chunks), the push/pull switch, the
+// frontier form and the launch shape are chosen by gas_batch_autotune.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,7 +19,7 @@
 
 #include "gas_gb300.h"
 #include "gas_gb300_core.h"
-#include "gas_gb300/detail/batch.cuh"
+#include "gas_gb300/detail/serve.cuh"
 #include "gas_internal.h"
 
 using gas::internal::CoreGraph;
@@ -27,6 +29,7 @@ using gas::internal::fail;
 namespace {
 
 constexpr int kMaxBatch = 256;  // queries per launch (8 words of query bits)
+constexpr int kKindPPR = 3;     // GraphCache kind of a PPR batch
 
 struct GraphCache {
   int kind, W, nQ, blocksPerSM, chunk, delta, pairs;
@@ -66,6 +69,12 @@ struct gas_batch_s {
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   float lastMs = 0.f;
   std::vector<GraphCache> graphs;
+  // personalised PageRank: the graph's PPR structures (built at the first
+  // PPR batch) and the batch state for rows of pprQP queries
+  gas::internal::PprGraph ppr;
+  int32_t pprRounds = 20;
+  unsigned char *pprState = nullptr;
+  int32_t pprQP = 0;
 };
 
 namespace {
@@ -112,6 +121,9 @@ void free_state(gas_batch *b) {
   }
   b->pairCap = 0;
   b->capQ = 0;
+  if (b->pprState) cudaFree(b->pprState);
+  b->pprState = nullptr;
+  b->pprQP = 0;
   drop_graphs(b);
 }
 
@@ -307,6 +319,191 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
   return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch transpose");
 }
 
+// ---- personalised PageRank batches
+// State of a batch with rows of QP queries: rank[2] | contrib[2] ([V][QP]
+// floats each) | partial ([slots][QP]) | arrive ([hubs]) | out ([QP][V]).
+size_t ppr_state_bytes(const gas_batch *b, const CoreGraph &g, int QP) {
+  const size_t V = (size_t)std::max(g.nV, 1);
+  return 4 * (5 * V * QP + (size_t)std::max(b->ppr.slots, 1) * QP + (size_t)std::max(b->ppr.hubs, 1)) + 256;
+}
+
+gas::detail::PprArgs ppr_args(gas_batch *b, const CoreGraph &g, int32_t nQ, int QP) {
+  gas::detail::PprArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nVertices = g.nV;
+  a.nQueries = nQ;
+  gas::detail::ppr_args_graph(a, g.inSrc, b->ppr.outDegree, b->ppr.lastActive, b->ppr.mem,
+                              b->ppr.units, b->ppr.slots);
+  const size_t V = (size_t)std::max(g.nV, 1);
+  float *p = reinterpret_cast<float *>(b->pprState);
+  a.rank[0] = p;
+  a.rank[1] = p + V * QP;
+  a.contrib[0] = p + 2 * V * QP;
+  a.contrib[1] = p + 3 * V * QP;
+  a.partial = p + 4 * V * QP;
+  a.arrive = reinterpret_cast<unsigned *>(a.partial + (size_t)std::max(b->ppr.slots, 1) * QP);
+  a.sources = b->srcDev;
+  a.teleport = 0.15f;
+  a.damp = 1.0f - a.teleport;  // as PPR::apply computes it, in float
+  return a;
+}
+
+float *ppr_out(gas_batch *b, const CoreGraph &g, int QP) {
+  const size_t V = (size_t)std::max(g.nV, 1);
+  return reinterpret_cast<float *>(b->pprState) + 4 * V * QP + (size_t)std::max(b->ppr.slots, 1) * QP +
+         (size_t)std::max(b->ppr.hubs, 1);
+}
+
+template <int QP>
+const void *ppr_run_fn() {
+  return (const void *)gas::detail::ppr_run_kernel<QP>;
+}
+
+const void *ppr_run_fn_for(int QP) {
+  switch (QP) {
+    case 1: return ppr_run_fn<1>();
+    case 2: return ppr_run_fn<2>();
+    case 4: return ppr_run_fn<4>();
+    case 8: return ppr_run_fn<8>();
+    case 16: return ppr_run_fn<16>();
+    case 32: return ppr_run_fn<32>();
+    case 64: return ppr_run_fn<64>();
+    case 128: return ppr_run_fn<128>();
+    default: return ppr_run_fn<256>();
+  }
+}
+
+template <int QP>
+void ppr_start(const gas::detail::PprArgs &a, int blocks, cudaStream_t s) {
+  gas::detail::ppr_init_kernel<QP><<<blocks, 256, 0, s>>>(a);
+  gas::detail::ppr_sources_kernel<QP><<<1, kMaxBatch, 0, s>>>(a);
+}
+
+void ppr_start_for(int QP, const gas::detail::PprArgs &a, int blocks, cudaStream_t s) {
+  switch (QP) {
+    case 1: ppr_start<1>(a, blocks, s); break;
+    case 2: ppr_start<2>(a, blocks, s); break;
+    case 4: ppr_start<4>(a, blocks, s); break;
+    case 8: ppr_start<8>(a, blocks, s); break;
+    case 16: ppr_start<16>(a, blocks, s); break;
+    case 32: ppr_start<32>(a, blocks, s); break;
+    case 64: ppr_start<64>(a, blocks, s); break;
+    case 128: ppr_start<128>(a, blocks, s); break;
+    default: ppr_start<256>(a, blocks, s); break;
+  }
+}
+
+// The whole PPR batch on b->stream: sources, arrival counters, initial
+// ranks, every round in one cooperative launch, query-major ranks in out.
+gas_status enqueue_ppr(gas_batch *b, const CoreGraph &g, int32_t nQ, int QP) {
+  cudaError_t e = cudaMemcpyAsync(b->srcDev, b->srcPinned, sizeof(int32_t) * nQ,
+                                  cudaMemcpyHostToDevice, b->stream);
+  gas::detail::PprArgs a = ppr_args(b, g, nQ, QP);
+  if (e == cudaSuccess && b->ppr.hubs > 0)
+    e = cudaMemsetAsync(a.arrive, 0, 4 * (size_t)b->ppr.hubs, b->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->ctl, 0, kCtlBytes, b->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "PPR batch reset");
+  ppr_start_for(QP, a, 4 * b->sms, b->stream);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "PPR batch init");
+  const void *fn = ppr_run_fn_for(QP);
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+  if (b->blocksPerSM > 0 && b->blocksPerSM < per) per = b->blocksPerSM;
+  const int blocks = std::max(per, 1) * std::max(b->sms, 1);
+  CtlView cv = ctl_view(b);
+  int rounds = b->pprRounds;
+  void *args[] = {&a, &rounds, &cv.bar, &cv.err, &cv.rounds};
+  e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(256), args, 0, b->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "PPR batch run launch");
+  dim3 tb(32, 8), tg((g.nV + 31) / 32, (QP + 31) / 32);
+  gas::detail::batch_transpose_kernel<<<tg, tb, 0, b->stream>>>(
+      reinterpret_cast<const int32_t *>(a.rank[rounds & 1]), g.nV, QP, nQ,
+      reinterpret_cast<int32_t *>(ppr_out(b, g, QP)));
+  e = cudaGetLastError();
+  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "PPR batch transpose");
+}
+
+gas_status run_one_ppr(gas_batch *b, const CoreGraph &g, int32_t nQ, const int32_t *sources,
+                       float *results, int32_t *rounds) {
+  int QP = 1;
+  while (QP < nQ) QP *= 2;
+  if (!b->ppr.mem) {
+    gas_status st = gas::internal::build_ppr_graph(g, b->sms, b->pprRounds, &b->ppr);
+    if (st) return st;
+  }
+  if (!b->srcDev) {  // the sources' device copy (also part of the BFS/SSSP state)
+    cudaError_t e = cudaMalloc(&b->srcDev, kMaxBatch * 4);
+    if (e != cudaSuccess) return cuda_fail(e, "PPR batch sources");
+    drop_graphs(b);
+  }
+  if (!b->pprState || b->pprQP < QP) {
+    if (b->pprState) cudaFree(b->pprState);
+    b->pprState = nullptr;
+    b->pprQP = 0;
+    drop_graphs(b);
+    cudaError_t e = cudaMalloc(&b->pprState, ppr_state_bytes(b, g, QP));
+    if (e != cudaSuccess) return cuda_fail(e, "PPR batch state");
+    b->pprQP = QP;
+  }
+  memcpy(b->srcPinned, sources, sizeof(int32_t) * nQ);
+  bool launched = false;
+  if (b->useGraphs) {
+    cudaGraphExec_t exec = nullptr;
+    for (auto &c : b->graphs)
+      if (c.kind == kKindPPR && c.W == QP && c.nQ == nQ && c.blocksPerSM == b->blocksPerSM &&
+          c.delta == b->pprRounds)
+        exec = c.exec;
+    if (!exec) {
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        gas_status cst = enqueue_ppr(b, g, nQ, QP);
+        cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+        if (cst == GAS_OK && ce == cudaSuccess && graph &&
+            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+          b->graphs.push_back({kKindPPR, QP, nQ, b->blocksPerSM, 0, b->pprRounds, 0, exec});
+        } else {
+          exec = nullptr;
+          b->useGraphs = false;  // this runtime cannot capture the batch: launch directly
+        }
+        if (graph) cudaGraphDestroy(graph);
+      } else {
+        b->useGraphs = false;
+      }
+      cudaGetLastError();
+    }
+    if (exec) {
+      cudaEventRecord(b->t0, b->stream);  // after any capture: device time only
+      cudaError_t e = cudaGraphLaunch(exec, b->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "PPR batch graph launch");
+      launched = true;
+    }
+  }
+  if (!launched) {
+    cudaEventRecord(b->t0, b->stream);
+    gas_status st = enqueue_ppr(b, g, nQ, QP);
+    if (st) return st;
+  }
+  cudaEventRecord(b->t1, b->stream);
+  CtlView cv = ctl_view(b);
+  int32_t re[2] = {0, 0};  // rounds, err
+  cudaError_t e = cudaMemcpyAsync(re, cv.rounds, 8, cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess && results)
+    e = cudaMemcpyAsync(results, ppr_out(b, g, QP), sizeof(float) * (size_t)nQ * g.nV,
+                        cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "PPR batch run");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->t0, b->t1);
+  b->lastMs += ms;
+  if (re[1]) {
+    cudaMemsetAsync(cv.err, 0, 4, b->stream);
+    return fail(GAS_ERR_TIMEOUT, "a bounded device wait of the batched PPR run timed out");
+  }
+  if (rounds) *rounds = std::max(*rounds, re[0]);
+  return GAS_OK;
+}
+
 gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const int32_t *sources,
                    int32_t *results, int32_t *rounds) {
   int32_t Q = 32;
@@ -319,7 +516,6 @@ gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const
     if (st) return st;
   }
   memcpy(b->srcPinned, sources, sizeof(int32_t) * nQ);
-  cudaEventRecord(b->t0, b->stream);
   bool launched = false;
   if (b->useGraphs) {
     cudaGraphExec_t exec = nullptr;
@@ -347,12 +543,14 @@ gas_status run_one(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ, const
       cudaGetLastError();
     }
     if (exec) {
+      cudaEventRecord(b->t0, b->stream);  // after any capture: device time only
       cudaError_t e = cudaGraphLaunch(exec, b->stream);
       if (e != cudaSuccess) return cuda_fail(e, "batch graph launch");
       launched = true;
     }
   }
   if (!launched) {
+    cudaEventRecord(b->t0, b->stream);
     st = enqueue_batch(b, g, kind, nQ, Q, pairs);
     if (st) return st;
   }
@@ -428,6 +626,7 @@ gas_status gas_batch_destroy(gas_batch *b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   free_state(b);
   free_units(b);
+  gas::internal::free_ppr_graph(&b->ppr);
   if (b->weightsOut) cudaFree(b->weightsOut);
   if (b->ctl) cudaFree(b->ctl);
   if (b->bucketMem) cudaFree(b->bucketMem);
@@ -445,6 +644,7 @@ gas_status gas_batch_set_graph(gas_batch *b, int32_t nVertices, int32_t nEdges,
   cudaSetDevice(b->device);
   free_state(b);
   free_units(b);
+  gas::internal::free_ppr_graph(&b->ppr);
   if (b->weightsOut) cudaFree(b->weightsOut);
   b->weightsOut = nullptr;
   gas_status st = gas_core_set_graph(b->core, nVertices, nEdges, srcs, dsts, weights,
@@ -467,9 +667,12 @@ gas_status gas_batch_set_config(gas_batch *b, int32_t chunkEdges, int32_t blocks
                                 int32_t useGraphs) {
   if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
   if (chunkEdges < 1 || blocksPerSM < 0) return fail(GAS_ERR_INVALID, "bad batch config");
+  const bool same = b->chunk == chunkEdges && b->blocksPerSM == blocksPerSM &&
+                    b->useGraphs == (useGraphs != 0);
   b->chunk = chunkEdges;
   b->blocksPerSM = blocksPerSM;
   b->useGraphs = useGraphs != 0;
+  if (same) return GAS_OK;  // captured batches stay valid
   drop_graphs(b);
   CoreGraph g;
   if (gas::internal::core_graph(b->core, &g)) return build_units(b, g, chunkEdges);
@@ -484,12 +687,14 @@ gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries, const 
   int kind;
   if (program == GAS_PROGRAM_BFS) {
     kind = gas::detail::kBatchBFS;
+  } else if (program == GAS_PROGRAM_PPR) {
+    kind = kKindPPR;
   } else if (program == GAS_PROGRAM_SSSP) {
     kind = gas::detail::kBatchSSSP;
     if (g.edgeBytes != 4 || !g.edgeData)
       return fail(GAS_ERR_STATE, "batched SSSP needs int32 edge weights in setGraph");
   } else {
-    return fail(GAS_ERR_UNSUPPORTED, "batched runs support BFS and SSSP");
+    return fail(GAS_ERR_UNSUPPORTED, "batched runs support BFS, SSSP and PPR");
   }
   if (nQueries < 0 || (nQueries > 0 && !sources)) return fail(GAS_ERR_INVALID, "bad sources");
   for (int32_t q = 0; q < nQueries; ++q)
@@ -500,8 +705,10 @@ gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries, const 
   if (rounds) *rounds = 0;
   for (int32_t q0 = 0; q0 < nQueries; q0 += kMaxBatch) {
     const int32_t nq = std::min(kMaxBatch, nQueries - q0);
-    gas_status st = run_one(b, g, kind, nq, sources + q0,
-                            results ? results + (size_t)q0 * g.nV : nullptr, rounds);
+    int32_t *res = results ? results + (size_t)q0 * g.nV : nullptr;
+    gas_status st = kind == kKindPPR
+                        ? run_one_ppr(b, g, nq, sources + q0, reinterpret_cast<float *>(res), rounds)
+                        : run_one(b, g, kind, nq, sources + q0, res, rounds);
     if (st) return st;
   }
   return GAS_OK;
@@ -510,6 +717,7 @@ gas_status gas_batch_run(gas_batch *b, int32_t program, int32_t nQueries, const 
 gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha) {
   if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
   if (alpha < 0) return fail(GAS_ERR_INVALID, "alpha must be >= 0");
+  if (b->alpha == alpha) return GAS_OK;
   b->alpha = alpha;
   drop_graphs(b);
   return GAS_OK;
@@ -518,6 +726,7 @@ gas_status gas_batch_set_policy(gas_batch *b, int32_t alpha) {
 gas_status gas_batch_set_delta(gas_batch *b, int32_t delta) {
   if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
   if (delta < 0) return fail(GAS_ERR_INVALID, "delta must be >= 0");
+  if (b->delta == delta) return GAS_OK;
   b->delta = delta;
   drop_graphs(b);
   return GAS_OK;
@@ -526,6 +735,7 @@ gas_status gas_batch_set_delta(gas_batch *b, int32_t delta) {
 gas_status gas_batch_set_frontier(gas_batch *b, int32_t mode) {
   if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
   if (mode < -1 || mode > 1) return fail(GAS_ERR_INVALID, "frontier mode must be -1, 0 or 1");
+  if (b->frontier == mode) return GAS_OK;
   b->frontier = mode;
   drop_graphs(b);
   return GAS_OK;
@@ -552,48 +762,88 @@ gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
   std::vector<int32_t> src(nq);
   std::mt19937 rng(12345);
   for (auto &s : src) s = (int32_t)(rng() % (uint32_t)std::max(g.nV, 1));
-  // SSSP: the bucket width first (Bellman-Ford rounds or delta-stepping),
-  // with the current launch configuration
-  if (program == GAS_PROGRAM_SSSP) {
-    const int32_t deltas[] = {0, 128, 512, 2048};
-    float bestD = 1e30f;
-    int32_t bd = b->delta;
-    for (int32_t d : deltas) {
-      gas_status st = gas_batch_set_delta(b, d);
-      int32_t r = 0;
-      if (st == GAS_OK) st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);
+  // time of one batch on these sources with the current settings (the first
+  // run of a shape warms up and captures its graph)
+  auto timed = [&](float *ms) -> gas_status {
+    int32_t r = 0;
+    gas_status st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);
+    if (st == GAS_OK) st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);
+    *ms = b->lastMs;
+    return st;
+  };
+  // one coordinate at a time: try each value, keep the fastest
+  auto tune = [&](const int32_t *vals, int n, gas_status (*set)(gas_batch *, int32_t),
+                  int32_t keep) -> gas_status {
+    float best = 1e30f;
+    int32_t bv = keep;
+    for (int i = 0; i < n; ++i) {
+      gas_status st = set(b, vals[i]);
+      float ms = 0.f;
+      if (st == GAS_OK) st = timed(&ms);
       if (st) return st;
-      if (b->lastMs < bestD) {
-        bestD = b->lastMs;
-        bd = d;
+      if (ms < best) {
+        best = ms;
+        bv = vals[i];
       }
     }
-    gas_status st = gas_batch_set_delta(b, bd);
-    if (st) return st;
+    return set(b, bv);
+  };
+  gas_status st = GAS_OK;
+  if (program != GAS_PROGRAM_PPR) {
+    // SSSP: the bucket width (Bellman-Ford rounds or delta-stepping)
+    if (program == GAS_PROGRAM_SSSP) {
+      const int32_t deltas[] = {0, 128, 512, 2048};
+      st = tune(deltas, 4, gas_batch_set_delta, b->delta);
+      if (st) return st;
+    }
+    // frontier form: (vertex, query) pairs where the graph allows them,
+    // else vertices with query masks; then, for masks, the push/pull switch
+    if (b->maxOutDeg <= 64) {
+      const int32_t forms[] = {-1, 0};
+      st = tune(forms, 2, gas_batch_set_frontier, b->frontier);
+      if (st) return st;
+    }
+    int32_t Q = 32;
+    while (Q < nq) Q *= 2;
+    if (!use_pairs(b, g, Q)) {
+      const int32_t alphas[] = {2, 10, 50};
+      st = tune(alphas, 3, gas_batch_set_policy, b->alpha);
+      if (st) return st;
+    }
   }
   const int32_t chunks[] = {32, 128, 512, 2048};
   const int32_t blocks[] = {0, 2, 1};
   float best = 1e30f;
   int32_t bc = b->chunk, bb = b->blocksPerSM;
-  for (int32_t c : chunks)
+  const int nc = program == GAS_PROGRAM_PPR ? 1 : 4;  // PPR's units are fixed (kPprChunk)
+  for (int i = 0; i < nc; ++i)
     for (int32_t k : blocks) {
-      gas_status st = gas_batch_set_config(b, c, k, b->useGraphs ? 1 : 0);
+      const int32_t c = program == GAS_PROGRAM_PPR ? b->chunk : chunks[i];
+      st = gas_batch_set_config(b, c, k, b->useGraphs ? 1 : 0);
+      float ms = 0.f;
+      if (st == GAS_OK) st = timed(&ms);
       if (st) return st;
-      int32_t r = 0;
-      st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);  // warm (and capture)
-      if (st) return st;
-      st = gas_batch_run(b, program, nq, src.data(), nullptr, &r);
-      if (st) return st;
-      if (b->lastMs < best) {
-        best = b->lastMs;
+      if (ms < best) {
+        best = ms;
         bc = c;
         bb = k;
       }
     }
-  gas_status st = gas_batch_set_config(b, bc, bb, b->useGraphs ? 1 : 0);
+  st = gas_batch_set_config(b, bc, bb, b->useGraphs ? 1 : 0);
   if (chunkOut) *chunkOut = bc;
   if (blocksOut) *blocksOut = bb;
   return st;
+}
+
+gas_status gas_batch_get_tuning(gas_batch *b, int32_t *chunkEdges, int32_t *blocksPerSM,
+                                int32_t *alpha, int32_t *frontier, int32_t *delta) {
+  if (!b) return fail(GAS_ERR_INVALID, "batch is NULL");
+  if (chunkEdges) *chunkEdges = b->chunk;
+  if (blocksPerSM) *blocksPerSM = b->blocksPerSM;
+  if (alpha) *alpha = b->alpha;
+  if (frontier) *frontier = b->frontier;
+  if (delta) *delta = b->delta;
+  return GAS_OK;
 }
 
 }  // extern "C"

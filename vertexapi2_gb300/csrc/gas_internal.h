@@ -69,5 +69,18 @@ struct BatchGraph {
 };
 bool batch_graph(struct gas_batch_s *b, BatchGraph *out);
 
+// Personalised PageRank structures of a graph (gas_serve.cu): out-degrees,
+// the pull work units (a vertex's in-edges, hubs cut into
+// gas::detail::kPprChunk-edge chunks with partial-sum slots) longest first,
+// and lastActive[v], the last of `rounds` rounds in which v is active.
+struct PprGraph {
+  int32_t *outDegree = nullptr;  // [V]
+  uint8_t *lastActive = nullptr; // [V]
+  int32_t *mem = nullptr;        // unitV | unitBeg | unitLen | unitSlot | slotFirst | slotCount | slotHub
+  int32_t units = 0, slots = 0, hubs = 0;
+};
+gas_status build_ppr_graph(const CoreGraph &g, int sms, int rounds, PprGraph *out);
+void free_ppr_graph(PprGraph *p);
+
 }  // namespace internal
 }  // namespace gas

@@ -77,10 +77,7 @@ struct ServeGraph {
   BatchGraph bg;
   // PPR: out-degrees, the last round each vertex is active, work units
   // (longest first) and the partial-sum slots of hub chunks
-  int32_t *outDegree = nullptr;   // [V]
-  uint8_t *lastActive = nullptr;  // [V]
-  int32_t *pprMem = nullptr;      // unitV | unitBeg | unitLen | unitSlot | slotFirst | slotCount | slotHub
-  int32_t pprUnits = 0, pprSlots = 0, pprHubs = 0;
+  gas::internal::PprGraph ppr;
   bool weighted = false;
   int32_t maxOutDeg = 0;         // pair frontier when small (lattice-like graphs)
   int32_t maxWeight = 0;
@@ -222,7 +219,7 @@ int64_t Server::state_bytes(const ServeGraph &g, int kind, int Q) const {
                         (use_pairs(g, kind, Q) ? 12 * V * Q : 0);
   if (kind == 0) return base + V * Q * 4 + 16 * V * W + lists;
   if (kind == 1) return base + V * Q * 4 + 12 * V * W + lists;
-  return base + V * Q * 16 + (int64_t)g.pprSlots * Q * 4 + (int64_t)g.pprHubs * 4;
+  return base + V * Q * 16 + (int64_t)g.ppr.slots * Q * 4 + (int64_t)g.ppr.hubs * 4;
 }
 
 int64_t Server::available_bytes() {
@@ -304,9 +301,7 @@ Server::~Server() {
   for (ServeGraph *g : graphs) {
     if (!g) continue;
     gas_batch_destroy(g->batch);
-    if (g->outDegree) cudaFree(g->outDegree);
-    if (g->lastActive) cudaFree(g->lastActive);
-    if (g->pprMem) cudaFree(g->pprMem);
+    gas::internal::free_ppr_graph(&g->ppr);
     delete g;
   }
   if (mirrors) cudaFreeHost(mirrors);
@@ -396,7 +391,7 @@ void Server::issue_chunk(int l, int rounds, bool final) {
     }
   } else if (b.kind == 2) {
     const int G = 32 / std::min(b.Q, 32);  // units per warp
-    const int blocks = round_blocks(*this, (b.g->pprUnits + G - 1) / G);
+    const int blocks = round_blocks(*this, (b.g->ppr.units + G - 1) / G);
     for (int k = 0; k < rounds; ++k) enqueue_ppr_round(b, b.roundsIssued + k, blocks);
     b.roundsIssued += rounds;
     launches += rounds;
@@ -463,25 +458,16 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     a.nVertices = V;
     a.nQueries = b.nQ;
     a.inSources = g.bg.g.inSrc;
-    a.outDegree = g.outDegree;
-    a.lastActive = g.lastActive;
-    const size_t nu = (size_t)std::max(g.pprUnits, 1), ns = (size_t)std::max(g.pprSlots, 1);
-    a.nUnits = g.pprUnits;
-    a.unitV = g.pprMem;
-    a.unitBeg = a.unitV + nu;
-    a.unitLen = a.unitBeg + nu;
-    a.unitSlot = a.unitLen + nu;
-    a.slotFirst = a.unitSlot + nu;
-    a.slotCount = a.slotFirst + ns;
-    a.slotHub = a.slotCount + ns;
+    gas::detail::ppr_args_graph(a, g.bg.g.inSrc, g.ppr.outDegree, g.ppr.lastActive, g.ppr.mem,
+                                g.ppr.units, g.ppr.slots);
     a.sources = b.sources;
     for (int k = 0; k < 2; ++k) {
       a.rank[k] = reinterpret_cast<float *>(take(Vs * b.Q * 4));
       a.contrib[k] = reinterpret_cast<float *>(take(Vs * b.Q * 4));
     }
-    a.partial = reinterpret_cast<float *>(take((size_t)g.pprSlots * b.Q * 4));
-    a.arrive = reinterpret_cast<unsigned *>(take((size_t)g.pprHubs * 4));
-    if (g.pprHubs > 0) cudaMemsetAsync(a.arrive, 0, (size_t)g.pprHubs * 4, b.stream);
+    a.partial = reinterpret_cast<float *>(take((size_t)g.ppr.slots * b.Q * 4));
+    a.arrive = reinterpret_cast<unsigned *>(take((size_t)g.ppr.hubs * 4));
+    if (g.ppr.hubs > 0) cudaMemsetAsync(a.arrive, 0, (size_t)g.ppr.hubs * 4, b.stream);
     if (p - b.state > b.stateBytes) return fail(GAS_ERR_STATE, "batch state layout overflow");
     a.teleport = 0.15f;
     a.damp = 1.0f - a.teleport;  // as PPR::apply computes it, in float
@@ -784,76 +770,10 @@ namespace {
 // PPR structures of a graph: out-degrees; work units (a vertex's in-edges,
 // hubs cut into kPprChunk-edge chunks with partial-sum slots), ordered
 // longest first by a counting sort; and lastActive[v], the last of the
-// kPprRounds rounds in which v is active, from kPprRounds - 1 pull steps
-// of the source-independent active sets on the device.
+// `rounds` rounds in which v is active, from rounds - 1 pull steps of the
+// source-independent active sets on the device.
 gas_status build_ppr(ServeGraph &g, int sms) {
-  constexpr int C = gas::detail::kPprChunk;
-  const int32_t V = g.bg.g.nV;
-  const std::vector<int32_t> &inOff = *g.bg.g.hInOff, &outOff = *g.bg.g.hOutOff;
-  std::vector<int32_t> deg((size_t)std::max(V, 1), 0);
-  for (int32_t v = 0; v < V; ++v) deg[v] = outOff[(size_t)v + 1] - outOff[v];
-  std::vector<int32_t> uv, ub, ul, us, sf, sc, sh;
-  uv.reserve(V);
-  ub.reserve(V);
-  ul.reserve(V);
-  us.reserve(V);
-  int32_t hubs = 0;
-  for (int32_t v = 0; v < V; ++v) {
-    const int32_t b = inOff[v], d = inOff[(size_t)v + 1] - b;
-    if (d <= C) {
-      uv.push_back(v); ub.push_back(b); ul.push_back(d); us.push_back(-1);
-      continue;
-    }
-    const int32_t n = (d + C - 1) / C, first = (int32_t)sf.size();
-    for (int32_t c = 0; c < n; ++c) {
-      uv.push_back(v); ub.push_back(b + c * C); ul.push_back(std::min(C, d - c * C));
-      us.push_back(first + c);
-      sf.push_back(first); sc.push_back(n); sh.push_back(hubs);
-    }
-    ++hubs;
-  }
-  const size_t nu = uv.size(), ns = sf.size();
-  // counting sort by length, longest first (stable)
-  std::vector<int64_t> pos((size_t)C + 2, 0);
-  for (size_t i = 0; i < nu; ++i) ++pos[(size_t)(C - ul[i]) + 1];
-  for (size_t k = 1; k < pos.size(); ++k) pos[k] += pos[k - 1];
-  std::vector<int32_t> mem(4 * std::max<size_t>(nu, 1) + 3 * std::max<size_t>(ns, 1), 0);
-  const size_t nuA = std::max<size_t>(nu, 1), nsA = std::max<size_t>(ns, 1);
-  for (size_t i = 0; i < nu; ++i) {
-    const size_t p = (size_t)pos[(size_t)(C - ul[i])]++;
-    mem[p] = uv[i];
-    mem[nuA + p] = ub[i];
-    mem[2 * nuA + p] = ul[i];
-    mem[3 * nuA + p] = us[i];
-  }
-  for (size_t i = 0; i < ns; ++i) {
-    mem[4 * nuA + i] = sf[i];
-    mem[4 * nuA + nsA + i] = sc[i];
-    mem[4 * nuA + 2 * nsA + i] = sh[i];
-  }
-  g.pprUnits = (int32_t)nu;
-  g.pprSlots = (int32_t)ns;
-  g.pprHubs = hubs;
-  uint8_t *tmp = nullptr;
-  const size_t Vs = (size_t)std::max(V, 1);
-  cudaError_t e = cudaMalloc(&g.outDegree, 4 * Vs);
-  if (e == cudaSuccess) e = cudaMalloc(&g.pprMem, 4 * mem.size());
-  if (e == cudaSuccess) e = cudaMalloc(&g.lastActive, Vs);
-  if (e == cudaSuccess) e = cudaMalloc(&tmp, 2 * Vs);
-  if (e == cudaSuccess) e = cudaMemcpy(g.outDegree, deg.data(), 4 * Vs, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(g.pprMem, mem.data(), 4 * mem.size(), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(g.lastActive, 0, Vs);
-  if (e == cudaSuccess) e = cudaMemset(tmp, 1, Vs);  // A0: every vertex
-  for (int k = 1; k < kPprRounds && e == cudaSuccess && V > 0; ++k) {
-    uint8_t *cur = tmp + ((k - 1) & 1) * Vs, *nxt = tmp + (k & 1) * Vs;
-    gas::detail::ppr_active_step_kernel<<<4 * sms, 256>>>(V, g.bg.g.inOff, g.bg.g.inSrc, cur, nxt,
-                                                           g.lastActive, k);
-    e = cudaGetLastError();
-  }
-  // the legacy default stream: ordered after the memsets, not with the lanes
-  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
-  if (tmp) cudaFree(tmp);
-  return e == cudaSuccess ? GAS_OK : cuda_fail(e, "PPR graph structures");
+  return gas::internal::build_ppr_graph(g.bg.g, sms, kPprRounds, &g.ppr);
 }
 
 }  // namespace
@@ -925,9 +845,7 @@ gas_status gas_server_add_graph(gas_server *h, int32_t nVertices, int32_t nEdges
   if (st == GAS_OK) st = build_ppr(*g, s.sms);
   if (st != GAS_OK) {
     gas_batch_destroy(g->batch);
-    if (g->outDegree) cudaFree(g->outDegree);
-    if (g->lastActive) cudaFree(g->lastActive);
-    if (g->pprMem) cudaFree(g->pprMem);
+    gas::internal::free_ppr_graph(&g->ppr);
     delete g;
     return st;
   }
@@ -1059,3 +977,92 @@ gas_status gas_server_get_stats(gas_server *h, gas_server_stats *st) {
 }
 
 }  // extern "C"
+
+namespace gas {
+namespace internal {
+
+gas_status build_ppr_graph(const CoreGraph &cg, int sms, int rounds, PprGraph *out) {
+  PprGraph &g = *out;
+  free_ppr_graph(out);
+  constexpr int C = gas::detail::kPprChunk;
+  const int32_t V = cg.nV;
+  const std::vector<int32_t> &inOff = *cg.hInOff, &outOff = *cg.hOutOff;
+  std::vector<int32_t> deg((size_t)std::max(V, 1), 0);
+  for (int32_t v = 0; v < V; ++v) deg[v] = outOff[(size_t)v + 1] - outOff[v];
+  std::vector<int32_t> uv, ub, ul, us, sf, sc, sh;
+  uv.reserve(V);
+  ub.reserve(V);
+  ul.reserve(V);
+  us.reserve(V);
+  int32_t hubs = 0;
+  for (int32_t v = 0; v < V; ++v) {
+    const int32_t b = inOff[v], d = inOff[(size_t)v + 1] - b;
+    if (d <= C) {
+      uv.push_back(v); ub.push_back(b); ul.push_back(d); us.push_back(-1);
+      continue;
+    }
+    const int32_t n = (d + C - 1) / C, first = (int32_t)sf.size();
+    for (int32_t c = 0; c < n; ++c) {
+      uv.push_back(v); ub.push_back(b + c * C); ul.push_back(std::min(C, d - c * C));
+      us.push_back(first + c);
+      sf.push_back(first); sc.push_back(n); sh.push_back(hubs);
+    }
+    ++hubs;
+  }
+  const size_t nu = uv.size(), ns = sf.size();
+  // counting sort by length, longest first (stable)
+  std::vector<int64_t> pos((size_t)C + 2, 0);
+  for (size_t i = 0; i < nu; ++i) ++pos[(size_t)(C - ul[i]) + 1];
+  for (size_t k = 1; k < pos.size(); ++k) pos[k] += pos[k - 1];
+  std::vector<int32_t> mem(4 * std::max<size_t>(nu, 1) + 3 * std::max<size_t>(ns, 1), 0);
+  const size_t nuA = std::max<size_t>(nu, 1), nsA = std::max<size_t>(ns, 1);
+  for (size_t i = 0; i < nu; ++i) {
+    const size_t p = (size_t)pos[(size_t)(C - ul[i])]++;
+    mem[p] = uv[i];
+    mem[nuA + p] = ub[i];
+    mem[2 * nuA + p] = ul[i];
+    mem[3 * nuA + p] = us[i];
+  }
+  for (size_t i = 0; i < ns; ++i) {
+    mem[4 * nuA + i] = sf[i];
+    mem[4 * nuA + nsA + i] = sc[i];
+    mem[4 * nuA + 2 * nsA + i] = sh[i];
+  }
+  g.units = (int32_t)nu;
+  g.slots = (int32_t)ns;
+  g.hubs = hubs;
+  uint8_t *tmp = nullptr;
+  const size_t Vs = (size_t)std::max(V, 1);
+  cudaError_t e = cudaMalloc(&g.outDegree, 4 * Vs);
+  if (e == cudaSuccess) e = cudaMalloc(&g.mem, 4 * mem.size());
+  if (e == cudaSuccess) e = cudaMalloc(&g.lastActive, Vs);
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, 2 * Vs);
+  if (e == cudaSuccess) e = cudaMemcpy(g.outDegree, deg.data(), 4 * Vs, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(g.mem, mem.data(), 4 * mem.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(g.lastActive, 0, Vs);
+  if (e == cudaSuccess) e = cudaMemset(tmp, 1, Vs);  // A0: every vertex
+  for (int k = 1; k < rounds && e == cudaSuccess && V > 0; ++k) {
+    uint8_t *cur = tmp + ((k - 1) & 1) * Vs, *nxt = tmp + (k & 1) * Vs;
+    gas::detail::ppr_active_step_kernel<<<4 * sms, 256>>>(V, cg.inOff, cg.inSrc, cur, nxt,
+                                                           g.lastActive, k);
+    e = cudaGetLastError();
+  }
+  // the legacy default stream: ordered after the memsets, not with the lanes
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (tmp) cudaFree(tmp);
+  if (e != cudaSuccess) {
+    free_ppr_graph(out);
+    return cuda_fail(e, "PPR graph structures");
+  }
+  return GAS_OK;
+}
+
+void free_ppr_graph(PprGraph *p) {
+  if (p->outDegree) cudaFree(p->outDegree);
+  if (p->lastActive) cudaFree(p->lastActive);
+  if (p->mem) cudaFree(p->mem);
+  *p = PprGraph();
+}
+
+}  // namespace internal
+}  // namespace gas

@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import check, load
+from ._lib import PROGRAM_PPR, check, load
 from .programs import EDGE_DTYPES, VERTEX_DTYPES
 
 
@@ -158,7 +158,8 @@ def device_supported(device: int = 0) -> bool:
 
 
 class GASBatch:
-    """Batched multi-source BFS / SSSP on one resident graph (gas_batch_*)."""
+    """Batched multi-source BFS / SSSP / personalised PageRank on one resident
+    graph (gas_batch_*)."""
 
     def __init__(self, device: int = 0, stream: int | None = None):
         self._lib = load()
@@ -195,12 +196,16 @@ class GASBatch:
         self.n_vertices = n_vertices
 
     def run(self, program: int, sources, want_results: bool = True):
+        """(results[nQueries][nVertices] or None, rounds): int32 depths or
+        distances, float32 PPR ranks."""
         src = np.ascontiguousarray(sources, dtype=np.int32)
         out = np.empty((src.shape[0], self.n_vertices), dtype=np.int32) if want_results else None
         rounds = C.c_int32()
         check(self._lib.gas_batch_run(self._h, program, int(src.shape[0]), _i32ptr(src),
                                       _i32ptr(out) if out is not None else None, C.byref(rounds)),
               "gas_batch_run")
+        if out is not None and program == PROGRAM_PPR:
+            out = out.view(np.float32)
         return out, rounds.value
 
     def set_config(self, chunk_edges: int = 256, blocks_per_sm: int = 0, use_graphs: bool = True):
@@ -226,6 +231,21 @@ class GASBatch:
         check(self._lib.gas_batch_autotune(self._h, program, n_queries, C.byref(c), C.byref(b)),
               "gas_batch_autotune")
         return c.value, b.value
+
+    def tuning(self) -> dict:
+        """The current settings (after autotune: the chosen ones)."""
+        v = [C.c_int32() for _ in range(5)]
+        check(self._lib.gas_batch_get_tuning(self._h, *[C.byref(x) for x in v]),
+              "gas_batch_get_tuning")
+        return dict(zip(("chunk", "blocks_per_sm", "alpha", "frontier", "delta"),
+                        (x.value for x in v)))
+
+    def set_tuning(self, t: dict) -> None:
+        """Restores settings read with tuning()."""
+        self.set_delta(t["delta"])
+        self.set_frontier(t["frontier"])
+        self.set_policy(t["alpha"])
+        self.set_config(t["chunk"], t["blocks_per_sm"], True)
 
     def last_ms(self) -> float:
         ms = C.c_float()
