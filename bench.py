@@ -501,9 +501,28 @@ def run_reference(args):
 
 
 # ------------------------------------------------------- plain workloads --
-def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
+def run_rounds(e, w, stepwise):
+    """One run() of a plain workload, or (stepwise) the same rounds through
+    countActive / gatherApply / scatterActivate / nextIter, the loop of the
+    reference's drivers (bfs.cu:98-108)."""
+    if not stepwise:
+        return e.run(w["max_iters"])
+    it = 0
+    e.set_iteration(0)
+    while (w["max_iters"] == 0 or it < w["max_iters"]) and e.count_active():
+        e.gather_apply(w["gather"])
+        e.scatter_activate(w["gather"])
+        e.next_iter()
+        it += 1
+        e.set_iteration(it)
+    return it
+
+
+def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True, stepwise=False):
     """One plain-engine workload: device-timed GTEPS, e2e through the C ABI,
-    roofline of the run's kernels, CPU baseline and oracle parity."""
+    roofline of the run's kernels, CPU baseline and oracle parity.  With
+    stepwise, every round is driven from the host (one gather/apply and one
+    scatter/activate launch per round) instead of run()'s persistent kernel."""
     import torch
     import vertexapi2_gb300 as gas
     w = make_workload(name)
@@ -521,7 +540,7 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
     def device_step():
         eng.restore_vertex_data()
         eng.set_active(lo, hi)
-        return eng.run(w["max_iters"])
+        return run_rounds(eng, w, stepwise)
 
     for _ in range(max(warmup, 1)):
         rounds = device_step()
@@ -547,13 +566,16 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
             eng.restore_vertex_data()
             ev[k][0].record(stream)
             eng.set_active(lo, hi)
-            eng.run(w["max_iters"])
+            run_rounds(eng, w, stepwise)
             ev[k][1].record(stream)
-            run_kernel_ms += eng.last_run_ms()  # the run kernels' own events
+            if not stepwise:
+                run_kernel_ms += eng.last_run_ms()  # the run kernels' own events
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     barrier(world)
     step_ms = [a.elapsed_time(b) for a, b in ev]
+    if stepwise:  # the rounds' kernels and the host round trips between them
+        run_kernel_ms = float(sum(step_ms))
     total_ms = allreduce_max(world, float(sum(step_ms)))
     all_edges = allreduce_sum(world, edges_per_run * steps)
     value = all_edges / (total_ms / 1e3) / 1e9
@@ -567,7 +589,7 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
     for _ in range(max(1, warmup)):
         e2e_eng.set_vertex_data(host_in)
         e2e_eng.set_active(lo, hi)
-        e2e_eng.run(w["max_iters"])
+        run_rounds(e2e_eng, w, stepwise)
         e2e_eng.get_results()
     barrier(world)
     torch.cuda.synchronize()
@@ -578,7 +600,7 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
         t0 = time.perf_counter()
         e2e_eng.set_vertex_data(host_in)
         e2e_eng.set_active(lo, hi)
-        e2e_eng.run(w["max_iters"])
+        run_rounds(e2e_eng, w, stepwise)
         e2e_eng.get_results()
         torch.cuda.synchronize()
         e2e_local += time.perf_counter() - t0
@@ -598,6 +620,11 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
     # active) + persistent run
     dense_first = (lo, hi) == (0, g.n_vertices)
     launches_per_step = 1 + (1 if w["gather"] else 0) + (1 if dense_first else 0)
+    kernel_label = ("run_dense_kernel + run_persistent_kernel" if dense_first
+                    else "run_persistent_kernel")
+    if stepwise:
+        launches_per_step = 2 * rounds
+        kernel_label = "gather_apply_kernel + scatter_activate_kernel (stepwise)"
 
     # CPU baseline (one core, the restatement) and parity with the oracle
     cpu, parity = None, None
@@ -635,11 +662,10 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True):
         "data": "synthetic",
         "config": workload_config(name, g),
         "run": {"rounds": rounds, "edges_traversed_per_run": edges_per_run,
+                "driver": "stepwise (host loop per round)" if stepwise else "run() (persistent)",
                 "l2": "flushed before every timed step, device-timed and end-to-end (512 MB write)",
                 "parallelism": f"replicas x{world}", "set_graph_ms": set_graph_ms},
-        "roofline": {"bound": "hbm",
-                     "kernel": "run_dense_kernel + run_persistent_kernel" if dense_first
-                     else "run_persistent_kernel", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": kernel_label, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
                      "traffic": (TRAFFIC_PER_LAUNCH.get(name)
@@ -1105,10 +1131,10 @@ def run_ours(args):
             return measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu)
         if name == "serve-c5":
             return measure_serve_c5(args, steps, warmup, world, rank, local, with_cpu)
-        return measure_plain(name, steps, warmup, world, rank, local, with_cpu)
+        return measure_plain(name, steps, warmup, world, rank, local, with_cpu, args.stepwise)
 
     line = measure(args.workload, args.steps, args.warmup)
-    if args.workload == HEADLINE and world == 1 and not args.no_per_algo:
+    if args.workload == HEADLINE and world == 1 and not args.no_per_algo and not args.stepwise:
         per = {}
         for name in PER_ALGO:
             t0 = time.perf_counter()
@@ -1133,6 +1159,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline and oracle legs")
     ap.add_argument("--no-per-algo", action="store_true",
                     help="headline workload only (no per_algo block)")
+    ap.add_argument("--stepwise", action="store_true",
+                    help="plain workloads: drive every round from the host (gatherApply / "
+                         "scatterActivate / nextIter) instead of run()")
     ap.add_argument("--rmat-scale", type=int, default=None,
                     help="smaller R-MAT scale for the R-MAT workloads (profiling captures)")
     ap.add_argument("--grid-side", type=int, default=1024,

@@ -7,17 +7,21 @@
 // gpugas.h:690-717, primitives/scatter_if_mgpu.h:130-157):
 //
 //   vertex v is active in round r+1  <=>  some in-neighbour u of v returned
-//   true in round r  (retStamp[r & 1][u] == stamp of round r)
+//   true in round r  (bit u of round r's frontier bitmap)
 //
 // which is exactly the set the reference's scatterActivate builds, so the
-// active sets and round counts are unchanged.  The stamps of consecutive
-// rounds live in two arrays, so a round reads the previous round's set
-// while it records its own.  The pass gathers speculatively, applies to the
-// active vertices and writes every vertex's data to the other buffer of a
-// ping-pong pair: no commit, no scatter traversal, no frontier list, one
-// grid barrier per round.  A list round with a large frontier can run the
-// same pass in mark mode: the active vertices are those the previous
-// scatter marked, and the others gather nothing.
+// active sets and round counts are unchanged.  The frontier of a dense
+// round is a bitmap of V bits (R-MAT-22: 512 KB, the reference keeps a byte
+// per vertex, gpugas.h:115): the round of stamp S sets the bits of its
+// apply-returned-true vertices in bitmap S % 3 (atomicOr, no return value),
+// reads bitmap (S - 1) % 3, and clears bitmap (S + 1) % 3, which no round
+// touches between its last read in round S - 1 and its first write in round
+// S + 1; so no round waits for a clear.  The pass gathers speculatively,
+// applies to the active vertices and writes every vertex's data to the
+// other buffer of a ping-pong pair: no commit, no scatter traversal, no
+// frontier list, one grid barrier per round.  A list round with a large
+// frontier can run the same pass in mark mode: the active vertices are
+// those the previous scatter marked, and the others gather nothing.
 //
 // Work units follow in-degree bins fixed per graph, each vertex owned by
 // one warp work unit, with no block barriers and no waits; warps take the
@@ -29,9 +33,15 @@
 //   in-degree > 1024    1024-edge chunks, one warp each; the warp that
 //                       finishes a vertex's last chunk (arrival counter)
 //                       combines the partials in chunk order.
-// Each vertex's reduction order depends only on its degree, so results are
-// identical run to run.
+// Source ids (and 4-byte edge data) are read as 16-byte words: the lanes of
+// a group take aligned quads of CSC positions, the one to three unaligned
+// edges at either end of a vertex's range one per lane; a one-thread vertex
+// reads the quads that cover its range.  Each vertex's reduction order
+// depends only on its degree and CSC position, so results are identical
+// run to run.
 #pragma once
+
+#include <cstring>
 
 #include "gather.cuh"
 
@@ -47,17 +57,19 @@ struct DenseCtx {
   const void *edgeData;
   const void *vdCur;
   void *vdNext;
-  const int32_t *prevRet;  // stamps written by the previous round (read only here)
-  int32_t *curRet;         // stamps of this round (the other array of the pair)
-  int32_t prevStamp;       // stamp of the previous round's apply-returned-true set
-  int32_t curStamp;
+  const uint32_t *prevBits;  // frontier bitmap of the previous round (read only here)
+  uint32_t *curBits;         // this round's apply-returned-true bits
   int32_t allActive;       // every vertex active (setActive(0, V))
   // Mark mode (a list round run as a pull pass): v is active iff
   // actMark[v] == markStamp (the previous round's scatter marks); inactive
-  // vertices gather nothing.  Null: activity from the in-neighbours' stamps.
+  // vertices gather nothing.  Null: activity from the in-neighbours' bits.
   const int32_t *actMark;
   int32_t markStamp;
-  int32_t skipStamps;      // allActive or mark mode: no per-edge stamp reads
+  // Active-set mode (a dense round after a fused round): v is active iff its
+  // bit is set in actBits, the bitmap the fused round activated; the others
+  // gather nothing.
+  const uint32_t *actBits;
+  int32_t skipBits;        // allActive, mark or active-set mode: no per-edge bitmap reads
   int32_t haveGather;
   int32_t iteration;
   unsigned long long *cnt;  // [3]: (active << 32 | in-edges), (ret << 32 | out-edges),
@@ -83,6 +95,20 @@ constexpr int kDenseCntStride = 4;  // counters per round (DenseCtx::cnt)
 constexpr int kDenseGrab = 4;  // work units a warp takes at a time
 constexpr int kSmallLanes = 8;     // lanes per vertex of in-degree 9..64
 
+// Frontier bitmaps: bit v of word v / 32.  Bits written by other SMs in the
+// previous round are read with plain loads after the grid barrier.
+__device__ __forceinline__ bool bit_test(const uint32_t *bits, int v) {
+  return (bits[v >> 5] >> (v & 31)) & 1u;
+}
+__device__ __forceinline__ void bit_set(uint32_t *bits, int v) {
+  atomicOr(bits + (v >> 5), 1u << (v & 31));  // result unused: a reduction, no round trip
+}
+// Clears nWords words of a bitmap, grid-stride.
+__device__ __forceinline__ void clear_bits(uint32_t *bits, int nWords) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nWords; i += stride) bits[i] = 0u;
+}
+
 // Per-lane accumulators of one edge stream: reduction, "has an edge",
 // "some edge activates the vertex".
 template <typename GR>
@@ -92,18 +118,52 @@ struct EdgeAcc {
   GR val;
 };
 
+// Edge data read by quads: 4-byte EdgeData (SSSP weights) comes with the
+// source ids as one 16-byte word; other sizes are read edge by edge.
 template <class P>
-__device__ __forceinline__ void edge_step(const DenseCtx &a, int v, int e,
-                                          EdgeAcc<typename P::GatherResult> &x) {
+struct QuadEdgeData {
+  typedef typename P::EdgeData ED;
+  static constexpr bool value = !std::is_empty<ED>::value && sizeof(ED) == 4;
+};
+
+// One in-edge (source id src, edge data *ep) of vertex v.  known: the
+// vertex is already known active, its activity bit is not read.
+template <class P>
+__device__ __forceinline__ void edge_acc(const DenseCtx &a, int v, int src,
+                                         const typename P::EdgeData *ep, bool known,
+                                         EdgeAcc<typename P::GatherResult> &x) {
   typedef typename P::VertexData VD;
   const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
-  const int src = __ldg(a.inSources + e);
-  x.act |= (a.skipStamps || a.prevRet[src] == a.prevStamp) ? 1u : 0u;
+  x.act |= (known || bit_test(a.prevBits, src)) ? 1u : 0u;
   if (a.haveGather) {
-    const typename P::GatherResult m = P::gatherMap(vd + v, vd + src, edge_ptr<P>(a.edgeData, e));
+    const typename P::GatherResult m = P::gatherMap(vd + v, vd + src, ep);
     x.val = x.has ? P::gatherReduce(x.val, m) : m;
   }
   x.has = 1u;
+}
+
+// The four in-edges at CSC positions [4q, 4q + 4): source ids (and 4-byte
+// edge data) as 16-byte loads, activity bits and source data in flight
+// together.
+template <class P>
+__device__ __forceinline__ void quad_acc(const DenseCtx &a, int v, int q, bool known,
+                                         EdgeAcc<typename P::GatherResult> &x) {
+  typedef typename P::EdgeData ED;
+  const int4 s4 = __ldg(reinterpret_cast<const int4 *>(a.inSources) + q);
+  const int src[4] = {s4.x, s4.y, s4.z, s4.w};
+  if constexpr (QuadEdgeData<P>::value) {
+    const int4 w4 = __ldg(reinterpret_cast<const int4 *>(a.edgeData) + q);
+    const int w[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      ED e;
+      memcpy(&e, &w[k], sizeof(ED));
+      edge_acc<P>(a, v, src[k], &e, known, x);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) edge_acc<P>(a, v, src[k], edge_ptr<P>(a.edgeData, 4 * q + k), known, x);
+  }
 }
 
 // Ordered tree combine of lane accumulators within aligned groups of
@@ -126,39 +186,39 @@ __device__ __forceinline__ void group_reduce(EdgeAcc<typename P::GatherResult> &
   }
 }
 
-// Lane-strided walk of the edges [beg, end) of vertex v by a whole warp,
-// kStrideDepth edges per lane in flight: all source ids first, then their
-// stamps and data.  Once some lane has seen an activating in-neighbour the
-// vertex is known active and the remaining stamps are not read.
-constexpr int kStrideDepth = 4;
-
-template <class P>
-__device__ __forceinline__ void strided_edges(const DenseCtx &a, int v, int beg, int end,
-                                              EdgeAcc<typename P::GatherResult> &x) {
-  typedef typename P::VertexData VD;
-  constexpr int J = kStrideDepth;
-  const int lane = threadIdx.x & 31;
-  const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
-  bool known = a.skipStamps != 0;  // warp-uniform
-  for (int base = beg; base < end; base += J * 32) {
-    int src[J];
-#pragma unroll
-    for (int j = 0; j < J; ++j) {
-      const int e = base + lane + 32 * j;
-      src[j] = e < end ? __ldg(a.inSources + e) : -1;
+// The edges [beg, end) of vertex v walked by the W lanes of a group (sl:
+// lane in the group): lanes 0..2 take the unaligned head [beg, 4*ceil(beg/4)),
+// lanes 4..6 the unaligned tail, and aligned quads go round the group, one
+// 16-byte load of source ids per lane and step (W = 32: 128 edges a step;
+// once some lane has seen an activating in-neighbour the vertex is known
+// active and no more activity bits are read).  W = 8 groups cover at most
+// 64 edges: two steps.
+template <class P, int W>
+__device__ __forceinline__ void group_edges(const DenseCtx &a, int v, int beg, int end, int sl,
+                                            EdgeAcc<typename P::GatherResult> &x) {
+  const int qb = (beg + 3) >> 2, qe = end >> 2;
+  const int hEnd = min(end, qb << 2);
+  const int tBeg = max(qe << 2, hEnd);
+  bool known = a.skipBits != 0;  // group-uniform
+  if (sl < 3 && beg + sl < hEnd) {
+    const int e = beg + sl;
+    edge_acc<P>(a, v, __ldg(a.inSources + e), edge_ptr<P>(a.edgeData, e), known, x);
+  }
+  if (sl >= 4 && sl < 7 && tBeg + sl - 4 < end) {
+    const int e = tBeg + sl - 4;
+    edge_acc<P>(a, v, __ldg(a.inSources + e), edge_ptr<P>(a.edgeData, e), known, x);
+  }
+  if constexpr (W == 32) {
+    known = known || __any_sync(kFullMask, x.act != 0u);
+    for (int q0 = qb; q0 < qe; q0 += 32) {
+      if (q0 + sl < qe) quad_acc<P>(a, v, q0 + sl, known, x);
+      known = known || __any_sync(kFullMask, x.act != 0u);
     }
+  } else {
+    static_assert(W * 8 >= 64, "a group walks at most 64 edges in two steps");
 #pragma unroll
-    for (int j = 0; j < J; ++j) {
-      if (src[j] < 0) continue;
-      x.act |= (known || a.prevRet[src[j]] == a.prevStamp) ? 1u : 0u;
-      if (a.haveGather) {
-        const typename P::GatherResult m =
-            P::gatherMap(vd + v, vd + src[j], edge_ptr<P>(a.edgeData, base + lane + 32 * j));
-        x.val = x.has ? P::gatherReduce(x.val, m) : m;
-      }
-      x.has = 1u;
-    }
-    known = __any_sync(kFullMask, x.act != 0u);
+    for (int k = 0; k < 2; ++k)
+      if (qb + sl + W * k < qe) quad_acc<P>(a, v, qb + sl + W * k, known, x);
   }
 }
 
@@ -182,12 +242,13 @@ __device__ __forceinline__ void dense_finish(const DenseCtx &a, int v, unsigned 
   typedef typename P::VertexData VD;
   const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
   VD tmp = vd[v];
-  if (a.allActive || (a.actMark ? a.actMark[v] == a.markStamp : act != 0u)) {
+  if (a.allActive || (a.actMark ? a.actMark[v] == a.markStamp
+                                 : (a.actBits ? bit_test(a.actBits, v) : act != 0u))) {
     const bool r = do_apply<P>(&tmp, g, a.iteration);
     ++c.active;
     c.inEdges += (unsigned)inDeg;
     if (r) {
-      a.curRet[v] = a.curStamp;
+      bit_set(a.curBits, v);
       ++c.ret;
       c.outEdges += (unsigned)(a.outOffsets[v + 1] - a.outOffsets[v]);
     }
@@ -195,9 +256,11 @@ __device__ __forceinline__ void dense_finish(const DenseCtx &a, int v, unsigned 
   reinterpret_cast<VD *>(a.vdNext)[v] = tmp;
 }
 
-// Mark mode: v is not active this round (its edges are skipped).
+// Mark or active-set mode: v is not active this round (its edges are
+// skipped).
 __device__ __forceinline__ bool mark_inactive(const DenseCtx &a, int v) {
-  return a.actMark != nullptr && a.actMark[v] != a.markStamp;
+  if (a.actMark) return a.actMark[v] != a.markStamp;
+  return a.actBits != nullptr && !bit_test(a.actBits, v);
 }
 
 // Warp work units of one dense pass: [large-vertex chunks | one vertex per
@@ -221,7 +284,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     const int v = a.chunkVertex[ch];
     const int beg = a.chunkBegin[ch];
     const int end = mark_inactive(a, v) ? beg : min(beg + kChunkEdges, a.inOffsets[v + 1]);
-    strided_edges<P>(a, v, beg, end, x);
+    group_edges<P, 32>(a, v, beg, end, lane, x);
     group_reduce<P, 32>(x);
     unsigned last = 0u;
     if (lane == 0) {
@@ -270,7 +333,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     // ---- one vertex per warp (in-degree 65..1024)
     const int v = a.binMid[u];
     const int beg = a.inOffsets[v], end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
-    strided_edges<P>(a, v, beg, end, x);
+    group_edges<P, 32>(a, v, beg, end, lane, x);
     group_reduce<P, 32>(x);
     if (lane == 0) dense_finish<P>(a, v, x.act, combined_result<P>(a, x), end - beg, c);
     return;
@@ -287,11 +350,7 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
       beg = a.inOffsets[v];
       end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
     }
-#pragma unroll
-    for (int k = 0; k < 64 / kSmallLanes; ++k) {
-      const int e = beg + sl + k * kSmallLanes;
-      if (e < end) edge_step<P>(a, v, e, x);
-    }
+    group_edges<P, kSmallLanes>(a, v, beg, end, sl, x);
     group_reduce<P, kSmallLanes>(x);
     if (sl == 0 && v >= 0) dense_finish<P>(a, v, x.act, combined_result<P>(a, x), end - beg, c);
     return;
@@ -306,16 +365,36 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     const int beg = a.inOffsets[v], end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
     typedef typename P::VertexData VD;
     const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
+    // the (at most three) 16-byte quads of source ids covering [beg, end);
+    // the edge arrays are padded to whole quads
+    static_assert(GAS_TPV_MAX_DEGREE == 8, "three quads cover 8 edges at any alignment");
+    int w[12];
+    const int q0 = beg >> 2, nq = end > beg ? ((end - 1) >> 2) - q0 + 1 : 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      int4 t = make_int4(0, 0, 0, 0);
+      if (k < nq) t = __ldg(reinterpret_cast<const int4 *>(a.inSources) + q0 + k);
+      w[4 * k] = t.x;
+      w[4 * k + 1] = t.y;
+      w[4 * k + 2] = t.z;
+      w[4 * k + 3] = t.w;
+    }
+    const int off = beg & 3;
     int src[GAS_TPV_MAX_DEGREE];
 #pragma unroll
-    for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k)
-      src[k] = beg + k < end ? __ldg(a.inSources + beg + k) : 0;
+    for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k) {
+      int x0 = w[k];
+      x0 = off == 1 ? w[k + 1] : x0;
+      x0 = off == 2 ? w[k + 2] : x0;
+      x0 = off == 3 ? w[k + 3] : x0;
+      src[k] = x0;
+    }
     GR g = gz;
     unsigned act = 0u;
 #pragma unroll
     for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k)
       if (beg + k < end) {
-        act |= (a.skipStamps || a.prevRet[src[k]] == a.prevStamp) ? 1u : 0u;
+        act |= (a.skipBits || bit_test(a.prevBits, src[k])) ? 1u : 0u;
         if (a.haveGather)
           g = P::gatherReduce(g, P::gatherMap(vd + v, vd + src[k], edge_ptr<P>(a.edgeData, beg + k)));
       }
@@ -369,17 +448,17 @@ __device__ void dense_pass(const DenseCtx &a) {
   dense_flush(a, c);
 }
 
-// Dense -> list transition: the vertices stamped in this round become the
-// scatter list (out-degree prefix, CSR begin), in vertex order per block.
+// Dense -> list transition: the vertices whose bits this round set become
+// the scatter list (out-degree prefix, CSR begin), in vertex order per block.
 template <int NT, int KS>
-__device__ void compact_ret(const int32_t *retStamp, int32_t stamp, const int32_t *outOffsets,
+__device__ void compact_ret(const uint32_t *bits, const int32_t *outOffsets,
                             int32_t nVertices, const gas_vertex_list &out, int32_t maxSplit,
                             unsigned *errWord, AppendSmem<NT, KS> &sm) {
   for (int base = blockIdx.x * NT; base < nVertices; base += gridDim.x * NT) {
     const int v = base + threadIdx.x;
     bool ok[1] = {false};
     int32_t ov[1] = {v}, od[1] = {0}, ob[1] = {0};
-    if (v < nVertices && retStamp[v] == stamp) {
+    if (v < nVertices && bit_test(bits, v)) {
       ok[0] = true;
       ob[0] = outOffsets[v];
       od[0] = outOffsets[v + 1] - ob[0];
@@ -388,22 +467,20 @@ __device__ void compact_ret(const int32_t *retStamp, int32_t stamp, const int32_
   }
 }
 
-// compact_ret as a kernel of its own (a frontier left as stamps by a run
+// compact_ret as a kernel of its own (a frontier left as a bitmap by a run
 // that stopped before a dense round, turned into a list when needed).
-static __global__ void __launch_bounds__(256) compact_ret_kernel(const int32_t *retStamp, int32_t stamp,
+static __global__ void __launch_bounds__(256) compact_ret_kernel(const uint32_t *bits,
                                                                  const int32_t *outOffsets, int32_t nVertices,
                                                                  gas_vertex_list out, int32_t maxSplit,
                                                                  unsigned *errWord) {
   __shared__ AppendSmem<256, 1> sm;
-  compact_ret<256, 1>(retStamp, stamp, outOffsets, nVertices, out, maxSplit, errWord, sm);
+  compact_ret<256, 1>(bits, outOffsets, nVertices, out, maxSplit, errWord, sm);
 }
 
-// List -> dense transition: stamp the vertices of a scatter list.
-__device__ __forceinline__ void stamp_list(const gas_vertex_list &l, int n, int32_t *retStamp,
-                                           int32_t stamp) {
+// List -> dense transition: the vertices of a scatter list into a bitmap.
+__device__ __forceinline__ void bits_from_list(const gas_vertex_list &l, int n, uint32_t *bits) {
   const int stride = gridDim.x * blockDim.x;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-    retStamp[l.vid[i]] = stamp;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) bit_set(bits, l.vid[i]);
 }
 
 }  // namespace detail

@@ -1,8 +1,23 @@
-// Fused list rounds for graphs whose in- and out-degrees are all <= 8
-// (lattices, road networks): a thread per frontier vertex gathers, applies
+// Fused rounds for graphs whose in- and out-degrees are all <= 8
+// (lattices, road networks): a thread per active vertex gathers, applies
 // and activates its out-neighbours in one phase, so a round costs one grid
 // barrier instead of two (gather -> barrier -> commit + scatter ->
 // barrier).
+//
+// The frontier of a fused round is a bitmap of V bits.  Activation is one
+// atomicOr per out-edge into the next round's bitmap (no return value, so
+// nothing waits on it), which also deduplicates: no activation stamps, no
+// list append, no counter that every warp contends for.  The round of
+// stamp S reads bitmap S % 3, sets bits in bitmap (S + 1) % 3 and clears
+// bitmap (S + 2) % 3 (every round of a run clears one ahead, whatever its
+// kind, so the bitmap a round writes is always clean).  Each block owns the
+// bitmap words b, b + grid, b + 2 * grid, ... (interleaved, so a spatially
+// clustered wavefront spreads over all blocks); it reads them, lists their
+// set bits in shared memory with a block scan, and its threads take the
+// listed vertices.  The first fused round after a list round (or a range)
+// reads that list instead, dealing its entries across all blocks.  Round
+// counts come from per-block sums of (active, in-edges, returned,
+// out-edges), added once per block.
 //
 // Bulk-synchronous reads without a commit step: for the fused rounds of a
 // run, vertex data moves into cells, one per vertex,
@@ -18,6 +33,7 @@
 // the run.
 #pragma once
 
+#include "dense.cuh"
 #include "gather.cuh"
 #include "scatter.cuh"
 
@@ -35,7 +51,12 @@ struct FusedCtx {
   void *cells;          // [V] FusedCell<VD> (Programs with a gather)
   void *vd;             // the run's vertex data (apply-only Programs update it in place)
   uint32_t stamp;       // this round's stamp
-  int32_t *retStamp;    // [V] stamp of the round whose apply returned true
+  uint32_t *nextBits;   // the next round's frontier bitmap (activated vertices)
+};
+
+// A fused round's counts, added once per block.
+struct FusedCounts {
+  unsigned active, inEdges, ret, outEdges;
 };
 
 // One cell, read from L2 (written by other CTAs) with 16-byte loads.
@@ -76,103 +97,170 @@ __device__ void fused_enter(const FusedCtx &f, const void *vd, int nVertices) {
   }
 }
 
-// Frontiers of at most this many vertices append per warp (one atomic per
-// warp, no block barrier); larger ones per block (one atomic per block, two
-// block barriers).
-constexpr int kWarpAppendMax = 16384;
-
-// Frontier entry i (none when i >= n) for this thread.  Counts this round's
-// apply-returned-true vertices and their out-edges into cRet / cOut.
-// warpAppend (block-uniform): append the activated vertices per warp.
-// Every thread of the block calls it (the appends are collective).
+// Vertex v (in-degree deg from CSC position beg; deg < 0: read from the
+// CSC offsets) in a fused round: gather from the in-neighbours' cells,
+// apply, write the cell, and when apply returns true set the out-
+// neighbours' bits in the next frontier.
 template <class P>
-__device__ __forceinline__ void fused_tpv_tile(const gas_gather_args &a, const ScatterArgs &sa, const FusedCtx &f,
-                               int i, int n, int T, bool warpAppend, unsigned &cRet, unsigned &cOut) {
+__device__ __forceinline__ void fused_vertex(const gas_gather_args &a, const ScatterArgs &sa,
+                                             const FusedCtx &f, int v, int beg, int deg,
+                                             FusedCounts &c) {
   typedef typename P::VertexData VD;
   typedef typename P::GatherResult GR;
   constexpr int D = GAS_TPV_MAX_DEGREE;
-  bool isEdge[D];
-  int32_t dst[D];
-#pragma unroll
-  for (int k = 0; k < D; ++k) {
-    isEdge[k] = false;
-    dst[k] = 0;
+  if (deg < 0) {
+    beg = a.inOffsets[v];
+    deg = a.inOffsets[v + 1] - beg;
   }
-  if (i < n) {
-    int v, pre, end, beg;
-    front_entry(a, i, n, T, v, pre, end, beg);
-    const int deg = end - pre;
-    const int obeg = a.outOffsets[v], oend = a.outOffsets[v + 1];
-    FusedCell<VD> *cell = reinterpret_cast<FusedCell<VD> *>(f.cells) + v;
-    int own = 0;
-    VD tmp;
-    if (a.haveGather) {
-      const FusedCell<VD> c = load_cell(cell);
-      own = (int)(c.ver & 1u);  // v is applied once per round: its word is still old
-      tmp = own ? c.s[1] : c.s[0];
-    } else {
-      tmp = reinterpret_cast<const VD *>(f.vd)[v];
-    }
-    // out-neighbours loaded before apply decides whether they are activated
-    const int odeg = oend - obeg;
-    int32_t outd[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) outd[k] = k < odeg ? __ldg(sa.outDests + obeg + k) : 0;
-    bool r;
-    if (a.haveGather) {
-      int src[D];
-#pragma unroll
-      for (int k = 0; k < D; ++k) src[k] = k < deg ? __ldg(a.inSources + beg + k) : 0;
-      VD sv[D];
-#pragma unroll
-      for (int k = 0; k < D; ++k)
-        if (k < deg) sv[k] = fused_read<VD>(f, src[k]);
-      GR acc = P::gatherZero;
-#pragma unroll
-      for (int k = 0; k < D; ++k)
-        if (k < deg)
-          acc = P::gatherReduce(acc, P::gatherMap(&tmp, &sv[k], edge_ptr<P>(a.edgeData, beg + k)));
-      r = do_apply<P>(&tmp, acc, a.iteration);
-      cell->s[own ^ 1] = tmp;
-      cell->ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
-    } else {  // apply only: nothing reads other vertices, update in place
-      const GR gz = P::gatherZero;
-      r = do_apply<P>(&tmp, gz, a.iteration);
-      reinterpret_cast<VD *>(f.vd)[v] = tmp;
-    }
-    if (r) {
-      f.retStamp[v] = (int32_t)f.stamp;
-      ++cRet;
-      cOut += (unsigned)(oend - obeg);
-#pragma unroll
-      for (int k = 0; k < D; ++k) {
-        isEdge[k] = k < odeg;
-        dst[k] = outd[k];
-      }
-    }
+  const int obeg = a.outOffsets[v], oend = a.outOffsets[v + 1];
+  FusedCell<VD> *cell = reinterpret_cast<FusedCell<VD> *>(f.cells) + v;
+  int own = 0;
+  VD tmp;
+  if (a.haveGather) {
+    const FusedCell<VD> cv = load_cell(cell);
+    own = (int)(cv.ver & 1u);  // v is applied once per round: its word is still old
+    tmp = own ? cv.s[1] : cv.s[0];
+  } else {
+    tmp = reinterpret_cast<const VD *>(f.vd)[v];
   }
-  // activation: in-degree, CSC begin and the stamp exchange in one round trip
-  bool ok[D];
-  int32_t dg[D], bg[D];
+  // out-neighbours loaded before apply decides whether they are activated
+  const int odeg = oend - obeg;
+  int32_t outd[D];
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
-    ok[k] = false;
-    dg[k] = 0;
-    bg[k] = 0;
-    if (isEdge[k]) {
-      bg[k] = sa.inOffsets[dst[k]];
-      dg[k] = sa.inOffsets[dst[k] + 1];
-      ok[k] = atomicExch(sa.mark + dst[k], sa.stamp) != sa.stamp;
+  for (int k = 0; k < D; ++k) outd[k] = k < odeg ? __ldg(sa.outDests + obeg + k) : 0;
+  bool r;
+  if (a.haveGather) {
+    int src[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) src[k] = k < deg ? __ldg(a.inSources + beg + k) : 0;
+    VD sv[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      if (k < deg) sv[k] = fused_read<VD>(f, src[k]);
+    GR acc = P::gatherZero;
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      if (k < deg)
+        acc = P::gatherReduce(acc, P::gatherMap(&tmp, &sv[k], edge_ptr<P>(a.edgeData, beg + k)));
+    r = do_apply<P>(&tmp, acc, a.iteration);
+    cell->s[own ^ 1] = tmp;
+    cell->ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
+  } else {  // apply only: nothing reads other vertices, update in place
+    const GR gz = P::gatherZero;
+    r = do_apply<P>(&tmp, gz, a.iteration);
+    reinterpret_cast<VD *>(f.vd)[v] = tmp;
+  }
+  ++c.active;
+  c.inEdges += (unsigned)deg;
+  if (r) {
+    ++c.ret;
+    c.outEdges += (unsigned)odeg;
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      if (k < odeg) bit_set(f.nextBits, outd[k]);
+  }
+}
+
+// A fused round whose frontier is a list (or the range of setActive): the
+// entries dealt across all blocks (entry base + k * grid + block), so a
+// frontier of a few tiles still spreads its loads over every SM.
+template <class P>
+__device__ __forceinline__ void fused_list_round(const gas_gather_args &a, const ScatterArgs &sa,
+                                                 const FusedCtx &f, int n, int T, FusedCounts &c) {
+  const int per = gridDim.x * blockDim.x;
+  for (int base = 0; base < n; base += per) {
+    const int i = base + (int)threadIdx.x * (int)gridDim.x + (int)blockIdx.x;
+    if (i < n) {
+      int v, pre, end, beg;
+      front_entry(a, i, n, T, v, pre, end, beg);
+      fused_vertex<P>(a, sa, f, v, beg, end - pre, c);
     }
   }
-#pragma unroll
-  for (int k = 0; k < D; ++k) dg[k] -= bg[k];
-  // the next round is fused again: one thread per entry, every degree <= 8
-  // (no split hints, no maximum degree)
-  if (warpAppend)
-    warp_append_list<D, false>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
-  else
-    block_append_list<D, false>(ok, dst, dg, bg, sa.next, a.capacity, a.errWord);
+}
+
+// Bitmap words a block reads per pass, and the shared-memory list of their
+// set bits (every bit set: 32 vertices a word).
+template <int NT>
+struct FusedBitsSmem {
+  int32_t vid[NT * 32];
+  ScanU64Smem<NT> scan;
+};
+
+// A fused round whose frontier is bitmap `bits` (nWords words): block b
+// reads words b + grid * k, NT at a time; a block scan of their bit counts
+// places the set bits' vertices in shared memory in vertex order per word,
+// and the block's threads take them.  Every thread of the block calls it.
+template <class P, int NT>
+__device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const ScatterArgs &sa,
+                                                 const FusedCtx &f, const uint32_t *bits, int nWords,
+                                                 FusedBitsSmem<NT> &sm, FusedCounts &c) {
+  const int G = gridDim.x;
+  const int perBlock = (nWords - (int)blockIdx.x + G - 1) / G;  // words this block owns
+  for (int k0 = 0; k0 < perBlock; k0 += NT) {  // block-uniform
+    const int k = k0 + (int)threadIdx.x;
+    const int w = (int)blockIdx.x + G * k;
+    const uint32_t word = k < perBlock ? bits[w] : 0u;
+    const unsigned long long mine = (unsigned long long)__popc(word);
+    unsigned long long excl, total;
+    block_exclusive_scan_u64<NT>(mine, excl, total, sm.scan);
+    if (total == 0ull) continue;  // block-uniform (the scan ends with a barrier)
+    int off = (int)excl;
+    uint32_t rest = word;
+    while (rest) {
+      const int b = __ffs(rest) - 1;
+      rest &= rest - 1u;
+      sm.vid[off++] = w * 32 + b;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < (int)total; i += NT) fused_vertex<P>(a, sa, f, sm.vid[i], 0, -1, c);
+    __syncthreads();  // sm.vid is rewritten by the next pass
+  }
+}
+
+// Adds the block's fused-round counts into cnt[0] = (active << 32 |
+// in-edges) and cnt[1] = (returned << 32 | out-edges): one atomic each per
+// block.  Every thread of the block calls it.
+__device__ __forceinline__ void fused_flush(const FusedCounts &c, unsigned long long *cnt) {
+  __shared__ unsigned long long sA[32], sR[32];
+  const unsigned wA = __reduce_add_sync(kFullMask, c.active);
+  const unsigned wEin = __reduce_add_sync(kFullMask, c.inEdges);
+  const unsigned wR = __reduce_add_sync(kFullMask, c.ret);
+  const unsigned wEout = __reduce_add_sync(kFullMask, c.outEdges);
+  if ((threadIdx.x & 31) == 0) {
+    sA[threadIdx.x >> 5] = ((unsigned long long)wA << 32) | wEin;
+    sR[threadIdx.x >> 5] = ((unsigned long long)wR << 32) | wEout;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long x = 0ull, y = 0ull;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      x += sA[k];
+      y += sR[k];
+    }
+    if (x) atomicAdd(cnt, x);
+    if (y) atomicAdd(cnt + 1, y);
+  }
+}
+
+// A frontier left in bitmap `bits` becomes the list `out` (in-degree
+// prefix, CSC begin, the gather's tile splits and maximum degree), in
+// vertex order per block: for a run that stops at maxRounds after a fused
+// round, whose caller continues from a list.
+template <int NT, int KS>
+__device__ void compact_active(const uint32_t *bits, const int32_t *inOffsets, int32_t nVertices,
+                               const gas_vertex_list &out, int32_t maxSplit, int32_t capacity,
+                               unsigned *errWord, AppendSmem<NT, KS> &sm) {
+  for (int base = blockIdx.x * NT; base < nVertices; base += gridDim.x * NT) {
+    const int v = base + threadIdx.x;
+    bool ok[1] = {false};
+    int32_t ov[1] = {v}, od[1] = {0}, ob[1] = {0};
+    if (v < nVertices && bit_test(bits, v)) {
+      ok[0] = true;
+      ob[0] = inOffsets[v];
+      od[0] = inOffsets[v + 1] - ob[0];
+    }
+    block_append<NT, 1, GAS_GATHER_TILE>(ok, ov, od, ob, out, maxSplit, capacity, errWord, sm);
+  }
 }
 
 // Every vertex's newest value back into the run's vertex data (f.vd).

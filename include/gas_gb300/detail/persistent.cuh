@@ -13,9 +13,9 @@
 // a thread per frontier vertex gathers, applies and activates, then one
 // grid barrier.  Rounds whose predecessor activated many out-edges run dense (pull, see
 // dense.cuh): one pass of degree-binned warp units and one barrier.
-// Transitions build the other representation: list -> dense stamps the
-// scatter list, dense -> list compacts the stamped vertices into a scatter
-// list and pushes it.  A list round whose frontier has many in-edges runs
+// Transitions build the other representation: list -> dense sets the
+// scatter list's bits in the frontier bitmap, dense -> list compacts the
+// bitmap into a scatter list and pushes it.  A list round whose frontier has many in-edges runs
 // as a pull pass too, over the vertices the previous scatter marked.  A run
 // that starts with every vertex active may run its leading dense rounds in
 // run_dense_kernel, a kernel with a smaller register budget, first.
@@ -39,36 +39,32 @@ namespace detail {
 // ~2-4 s of polling before a grid barrier reports a timeout
 constexpr unsigned kBarrierSpinLimit = 1u << 25;
 
-// Grid-wide barrier of a cooperative launch.  bar (8-byte aligned) is one
-// 64-bit word, generation << 32 | arrivals (bar[0] arrivals, bar[1]
-// generation); arrivals must be 0 at launch.  Each block adds one arrival
-// and learns the generation from the same atomic; the last arrival starts
-// the next generation and clears the arrivals with one more atomic, which
-// nothing waits on, and the others poll the generation.  Returns false on
-// timeout or when another block reported one.
+// Grid-wide barrier of a cooperative launch on one 32-bit word (bar[0],
+// zero at launch; bar[1] unused).  Each block arrives with one atomic:
+// block 0 adds 2^31 - (gridDim.x - 1), every other block adds 1, so the
+// word's top bit flips exactly when the last block arrives, whichever that
+// is, and the low bits return to their value before the barrier.  A block
+// waits until the top bit differs from the one its own atomic returned: no
+// second atomic on the release path.  Returns false on timeout or when
+// another block reported one.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
   __shared__ unsigned s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned ok = 1u;
-    unsigned long long *word = reinterpret_cast<unsigned long long *>(bar);
     __threadfence();
-    const unsigned long long old = atomicAdd(word, 1ull);
-    const unsigned gen = (unsigned)(old >> 32);
-    if ((unsigned)old == gridDim.x - 1) {
-      atomicAdd(word, (1ull << 32) - gridDim.x);
-    } else {
-      unsigned spins = 0;
-      while (ld_acquire(bar + 1) == gen) {
-        ++spins;
-        if (spins > kBarrierSpinLimit ||
-            ((spins & 4095u) == 0 && (ld_acquire(errWord) & GAS_DEVERR_TIMEOUT))) {
-          atomicOr(errWord, GAS_DEVERR_TIMEOUT);
-          ok = 0u;
-          break;
-        }
-        __nanosleep(32);
+    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+    const unsigned old = atomicAdd(bar, add);
+    unsigned spins = 0;
+    while (((ld_acquire(bar) ^ old) & 0x80000000u) == 0u) {
+      ++spins;
+      if (spins > kBarrierSpinLimit ||
+          ((spins & 4095u) == 0 && (ld_acquire(errWord) & GAS_DEVERR_TIMEOUT))) {
+        atomicOr(errWord, GAS_DEVERR_TIMEOUT);
+        ok = 0u;
+        break;
       }
+      __nanosleep(32);
     }
     __threadfence();
     s_ok = ok;
@@ -81,6 +77,7 @@ template <class P>
 union PersistentSmem {
   GatherSmem<P> g;
   ScatterSmem s;
+  FusedBitsSmem<kGNT> fb;
 };
 
 // The fixed part of a dense pass's context (graph, degree bins, chunks).
@@ -111,21 +108,41 @@ __device__ __forceinline__ DenseCtx dense_ctx(const gas_run_args &ra) {
   return dc;
 }
 
+// The frontier bitmap of the round with this stamp (null when the run has
+// none: dense rounds disabled and no fused rounds).
+__device__ __forceinline__ uint32_t *round_bits(const gas_run_args &ra, int32_t stamp) {
+  return ra.retBits[0] ? ra.retBits[(unsigned)stamp % 3u] : nullptr;
+}
+
+// The active-set bitmap of the fused round with this stamp (see fused.cuh).
+__device__ __forceinline__ uint32_t *front_bits(const gas_run_args &ra, int32_t stamp) {
+  return ra.frontBits[(unsigned)stamp % 3u];
+}
+
+// Clears the bitmaps the rounds after this one write: the frontier bitmap
+// of the next round (dense.cuh) and the active-set bitmap of the round after
+// it (fused.cuh).  Every round of a run calls it, whatever its kind.
+__device__ __forceinline__ void clear_ahead(const gas_run_args &ra, int32_t stamp) {
+  if (ra.retBits[0]) clear_bits(round_bits(ra, stamp + 1), ra.bitWords);
+  if (ra.frontBits[0]) clear_bits(front_bits(ra, stamp + 2), ra.bitWords);
+}
+
 // Round r's per-round settings of a dense pass over vdBuf[vcur]; with
-// byMark, the active vertices are those round r-1's scatter marked.
+// byMark, the active vertices are those round r-1's scatter marked; with
+// actBits, those whose bits round r-1 (a fused round) set.
 __device__ __forceinline__ void dense_round(DenseCtx &dc, const gas_run_args &ra, void *const vdBuf[2],
-                                            int vcur, int r, bool allActive, bool byMark = false) {
+                                            int vcur, int r, bool allActive, bool byMark = false,
+                                            const uint32_t *actBits = nullptr) {
   const int32_t stamp = ra.stampBase + r;
   dc.vdCur = vdBuf[vcur];
   dc.vdNext = vdBuf[vcur ^ 1];
-  dc.prevRet = ra.retStamp[(r + 1) & 1];
-  dc.curRet = ra.retStamp[r & 1];
-  dc.prevStamp = stamp - 1;
-  dc.curStamp = stamp;
+  dc.prevBits = round_bits(ra, stamp - 1);
+  dc.curBits = round_bits(ra, stamp);
   dc.allActive = allActive ? 1 : 0;
   dc.actMark = byMark ? ra.mark : nullptr;
   dc.markStamp = stamp - 1;
-  dc.skipStamps = (allActive || byMark) ? 1 : 0;
+  dc.actBits = actBits;
+  dc.skipBits = (allActive || byMark || actBits) ? 1 : 0;
   dc.iteration = ra.g.iteration + r;
   dc.cnt = ra.denseCnt + kDenseCntStride * (r % 3);
 }
@@ -146,14 +163,14 @@ __device__ __forceinline__ void round_resets(const gas_run_args &ra, int r, int 
 }
 
 // Dense -> list transition at the end of dense round r (stamp): the
-// vertices stamped in it become scatL[sidx] (vertex order per block) and
-// are pushed into frontL[cur ^ 1].  False when a grid barrier gave up.
+// vertices whose bits it set become scatL[sidx] (vertex order per block)
+// and are pushed into frontL[cur ^ 1].  False when a grid barrier gave up.
 template <class P>
 __device__ __forceinline__ bool dense_to_list(const gas_run_args &ra, const gas_gather_args &a,
                                               ScatterArgs &sa, PersistentSmem<P> &sm, int r, int cur,
                                               int sidx) {
   const int32_t stamp = ra.stampBase + r;
-  compact_ret<kGNT, kGVT>(ra.retStamp[r & 1], stamp, a.outOffsets, a.nVertices, ra.scatL[sidx],
+  compact_ret<kGNT, kGVT>(round_bits(ra, stamp), a.outOffsets, a.nVertices, ra.scatL[sidx],
                           a.maxScatTiles, a.errWord, sm.g.app);
   if (!grid_barrier(ra.barrier, a.errWord)) return false;
   const unsigned long long sc = *ra.scatL[sidx].count;
@@ -198,6 +215,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_dense_kernel(const gas_ru
       break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, ra.cur ^ (r & 1), ra.sidx ^ (r & 1));
+    clear_ahead(ra, ra.stampBase + r);
     dense_round(dc, ra, vdBuf, vcur, r, r == 0);
     dense_pass<P>(dc);
     if (!grid_barrier(ra.barrier, ra.g.errWord)) {
@@ -270,6 +288,8 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
 
   int cur = ra.cur, sidx = ra.sidx, vcur = 0;
   bool versioned = false;  // the vertex data lives in the fused cells
+  bool frontBits = false;  // this round's active set is front_bits(stamp), not a list
+  bool capped = false;     // stopped at maxRounds
   bool rangeMode = a.rangeMode != 0;
   int mode = ra.allActive ? kDense : kList;
   bool allActive = ra.allActive != 0;
@@ -292,11 +312,13 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
     if (ended) break;
     if (ra.maxRounds > 0 && r >= ra.maxRounds) {
       denseEnd = mode == kDense;
+      capped = true;
       break;
     }
     const unsigned epoch = ra.epochBase + (unsigned)r;
     const int32_t stamp = ra.stampBase + r;
     if (blockIdx.x == 0 && threadIdx.x == 0) round_resets(ra, r, cur, sidx);
+    clear_ahead(ra, stamp);
     unsigned long long statA, statR;
     bool denseNext;
     bool byMark = false;  // a list round run as a pull pass over its marked frontier
@@ -309,51 +331,49 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       a.epoch = epoch;
       a.iteration = ra.g.iteration + r;
       a.vertexData = vdBuf[vcur];
-      frontier_size(a, n, T);
-      frontMaxDeg = frontier_max_degree(a);  // loaded together with the count
-      if (n == 0) break;  // uniform: every block read the same count
-      // A frontier whose in-edges are a large share of the graph gathers
-      // faster in a pull pass that skips the unmarked vertices.
-      byMark = r > 0 && !rangeMode && !versioned && a.haveGather && ra.denseAlpha > 0 &&
-               (long long)T * kMarkPullFactor > E;
+      if (!frontBits) {
+        frontier_size(a, n, T);
+        frontMaxDeg = frontier_max_degree(a);  // loaded together with the count
+        if (n == 0) break;  // uniform: every block read the same count
+        // A frontier whose in-edges are a large share of the graph gathers
+        // faster in a pull pass that skips the unmarked vertices.
+        byMark = r > 0 && !rangeMode && !versioned && a.haveGather && ra.denseAlpha > 0 &&
+                 (long long)T * kMarkPullFactor > E;
+      }
     }
+    bool nextBits = false;  // the next round's active set is front_bits(stamp + 1)
     if (mode == kList && !byMark) {
-      // ---------------- push round: list (or range) frontier
-      bool tpvG;
-      const int ntG = gather_tiles(a, n, T, frontMaxDeg, tpvG);
-      if (ra.fused && (tpvG || !a.haveGather)) {
+      // ---------------- push round: list (or range) frontier, or a bitmap
+      bool tpvG = true;
+      const int ntG = frontBits ? 0 : gather_tiles(a, n, T, frontMaxDeg, tpvG);
+      // fused rounds launch in the 2-CTA/SM instantiation only (launchRun)
+      if (MinBlocks <= 2 && ra.fused && (frontBits || tpvG || !a.haveGather)) {
         // ---------------- fused round: one phase, one barrier
         FusedCtx f;
         f.cells = ra.fusedCells;
         f.vd = vdBuf[vcur];
         f.stamp = (uint32_t)stamp;
-        f.retStamp = ra.retStamp[r & 1];
+        f.nextBits = front_bits(ra, stamp + 1);
         if (a.haveGather && !versioned) {  // the vertex data moves into the cells
           fused_enter<P>(f, vdBuf[vcur], a.nVertices);
           versioned = true;
           if (!grid_barrier(ra.barrier, a.errWord)) break;
         }
-        sa.next = ra.frontL[cur ^ 1];
-        sa.stamp = stamp;
-        unsigned cRet = 0u, cOut = 0u;
-        const bool warpAppend = n <= kWarpAppendMax;
-        // entries dealt across all blocks (entry base + k*grid + block), so a
-        // frontier of a few tiles still spreads its loads over every SM
-        const int per = gridDim.x * blockDim.x;
-        for (int base = 0; base < n; base += per) {
-          fused_tpv_tile<P>(a, sa, f, base + (int)threadIdx.x * (int)gridDim.x + (int)blockIdx.x, n, T,
-                            warpAppend, cRet, cOut);
-        }
-        cRet = __reduce_add_sync(kFullMask, cRet);
-        cOut = __reduce_add_sync(kFullMask, cOut);
-        unsigned long long *rc = ra.denseCnt + kDenseCntStride * (r % 3) + 1;
-        if ((threadIdx.x & 31) == 0 && cRet) atomicAdd(rc, ((unsigned long long)cRet << 32) | cOut);
+        FusedCounts fc = {0u, 0u, 0u, 0u};
+        if (frontBits)
+          fused_bits_round<P, kGNT>(a, sa, f, front_bits(ra, stamp), ra.bitWords, sm.fb, fc);
+        else
+          fused_list_round<P>(a, sa, f, n, T, fc);
+        unsigned long long *cnt = ra.denseCnt + kDenseCntStride * (r % 3);
+        fused_flush(fc, cnt);
         if (!grid_barrier(ra.barrier, a.errWord)) break;
-        statA = ((unsigned long long)n << 32) | (unsigned)T;
-        statR = *rc;
+        statA = cnt[0];
+        statR = cnt[1];
+        if ((statA >> 32) == 0) break;  // the bitmap was empty: the run ended before this round
         const int nr = (int)(statR >> 32);
         denseNext = ra.denseAlpha > 0 && nr > 0 &&
                     (long long)(statR & 0xffffffffull) * ra.denseAlpha > E;
+        nextBits = true;
         if (denseNext && versioned) {  // dense rounds read the vertex data array
           fused_fold<P>(f, a.nVertices);
           versioned = false;
@@ -390,7 +410,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       sa.stamp = stamp;
       if (a.haveGather) commit_frontier(sa, n);
       if (denseNext) {
-        stamp_list(a.scat, ns, ra.retStamp[r & 1], stamp);
+        bits_from_list(a.scat, ns, round_bits(ra, stamp));
       } else {
         bool tpvS;
         const int ntS = scatter_tiles(sa.scat, ns, Ts, tpvS);
@@ -414,7 +434,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       }  // two-phase round
     } else {
       // ---------------- pull round over every vertex
-      dense_round(dc, ra, vdBuf, vcur, r, allActive, byMark);
+      dense_round(dc, ra, vdBuf, vcur, r, allActive, byMark, frontBits ? front_bits(ra, stamp) : nullptr);
       dense_pass<P>(dc);
       if (!grid_barrier(ra.barrier, a.errWord)) break;
       statA = dc.cnt[0];
@@ -437,8 +457,21 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
     mode = denseNext ? kDense : kList;
     allActive = false;
     rangeMode = false;
+    frontBits = nextBits;
     cur ^= 1;
     sidx ^= 1;
+  }
+  if (capped && frontBits) {
+    // Stopped at maxRounds before a round whose active set is a bitmap:
+    // the caller continues from a list, so the bitmap becomes frontL[cur].
+    denseEnd = false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      *ra.frontL[cur].count = 0ull;
+      *ra.frontL[cur].maxDeg = 0u;
+    }
+    if (grid_barrier(ra.barrier, a.errWord))
+      compact_active<kGNT, kGVT>(front_bits(ra, ra.stampBase + r), a.inOffsets, a.nVertices,
+                                 ra.frontL[cur], ra.maxGatherTiles, a.capacity, a.errWord, sm.g.app);
   }
   if (versioned) {  // the newest values into the run's current buffer
     FusedCtx f;

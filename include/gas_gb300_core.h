@@ -119,12 +119,22 @@ typedef struct {
   int32_t maxRounds;          /* 0 = until no vertex is active              */
   unsigned epochBase;         /* carry-flag epoch of round 0                */
   int32_t stampBase;          /* activation stamp of round 0                */
-  unsigned *barrier;          /* [2]: arrival count, generation             */
+  unsigned *barrier;          /* [2]: [0] the grid barrier's arrival word (zero
+                                 at launch), [1] unused                       */
   int32_t *roundsOut;         /* rounds executed                            */
   /* dense (pull) rounds */
   void *vertexAlt;            /* second vertex-data buffer (ping-pong)      */
-  int32_t *retStamp[2];       /* [V] each: stamp of the round whose apply returned
-                                 true; round r writes [r & 1] and reads [(r-1) & 1] */
+  uint32_t *retBits[3];       /* frontier bitmaps, bitWords words each: bit v set when
+                                 v's apply returned true; the round of stamp S sets
+                                 bits in [S % 3], reads [(S-1) % 3] and clears
+                                 [(S+1) % 3]; [stampBase % 3] is clear at launch */
+  int32_t bitWords;           /* ceil(V / 32)                                */
+  uint32_t *frontBits[3];     /* active-set bitmaps of the fused rounds (null when
+                                 the graph has none), bitWords words each: the
+                                 round of stamp S reads [S % 3] (when its frontier
+                                 is a bitmap), sets the bits of the vertices it
+                                 activates in [(S+1) % 3] and clears [(S+2) % 3];
+                                 [(stampBase+1) % 3] is clear at launch */
   unsigned long long *denseCnt; /* [3][4] per-round counters: active/in-edges,
                                  ret/out-edges, dense work units taken, unused */
   int32_t denseAlpha;         /* next round dense when out-edges*alpha > E; 0 = never */
@@ -162,8 +172,8 @@ typedef struct {
   int32_t denseFirst;
   int32_t *resume;
   /* set to 1 when the run stopped at maxRounds before a dense round: the
-   * next frontier is then the vertices its last round stamped (retStamp)
-   * instead of a list */
+   * next frontier is then the vertices whose bits its last round set
+   * (retBits) instead of a list */
   int32_t *denseEndOut;
 } gas_run_args;
 

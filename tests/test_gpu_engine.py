@@ -487,3 +487,64 @@ def test_stepwise_after_run_stopped_before_dense_round(gpu, port):
                 done += 1
             e.get_results()
         assert np.array_equal(vd, ref) and done == st["iterations"], k
+
+
+@pytest.mark.parametrize("alpha", [0, 10, 5000])
+def test_fused_bitmap_rounds_match_oracle(gpu, port, alpha):
+    """Lattices run fused rounds whose frontier is a bitmap.  Results and
+    per-round counts equal the oracle's for SSSP (every vertex active at the
+    start: a dense first round, then fused rounds) and BFS (a one-vertex
+    range, then fused rounds); alpha = 5000 turns many fused rounds' successors
+    into dense rounds that take their active set from the fused round's
+    bitmap."""
+    g = graphs.grid(70, 55, 0.15, seed=95, weights=(1, 100))
+    nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
+    ref, st = port.sssp(nv, s, d, w, 0, stats_cap=4096)
+    got, rounds, gst = _run_policy(PROGRAM_SSSP, nv, s, d, P.sssp_init(nv, 0), w=w, alpha=alpha)
+    assert np.array_equal(got, ref) and rounds == st["iterations"]
+    for k in ("active", "gathered", "ret", "scattered"):
+        assert np.array_equal(gst[k][:rounds], st[k]), k
+    ref, st = port.bfs(nv, s, d, 5, stats_cap=4096)
+    got, rounds, gst = _run_policy(PROGRAM_BFS, nv, s, d, P.bfs_init(nv), active=(5, 6), alpha=alpha)
+    assert np.array_equal(got, ref) and rounds == st["iterations"]
+    for k in ("active", "gathered", "ret", "scattered"):
+        assert np.array_equal(gst[k][:rounds], st[k]), k
+
+
+@pytest.mark.parametrize("k", [1, 2, 5])
+def test_fused_run_resumes_across_calls(gpu, port, k):
+    """run(k) on a lattice stops with the next frontier in a bitmap; the run
+    turns it into a list before it returns, and the next call (or the
+    stepwise API) continues from that list."""
+    g = graphs.grid(40, 37, 0.15, seed=96, weights=(1, 100))
+    nv, s, d, w = g.n_vertices, g.srcs, g.dsts, g.weights
+    ref, st = port.sssp(nv, s, d, w, 0)
+    for alpha in (10, 5000):
+        vd = P.sssp_init(nv, 0)
+        with GASEngine(PROGRAM_SSSP) as e:
+            e.set_graph(nv, vd, s, d, w)
+            e.set_dense_policy(alpha)
+            e.set_active(0, nv)
+            done = 0
+            while True:
+                r = e.run(k)
+                done += r
+                if r < k:
+                    break
+            e.get_results()
+        assert np.array_equal(vd, ref) and done == st["iterations"], alpha
+    ref, st = port.bfs(nv, s, d, 0)
+    vd = P.bfs_init(nv)
+    with GASEngine(PROGRAM_BFS) as e:
+        e.set_graph(nv, vd, s, d)
+        e.set_active(0, 1)
+        done = e.run(k + 3)
+        e.set_iteration(done)
+        while e.count_active():  # stepwise from the list the capped run left
+            e.gather_apply(False)
+            e.scatter_activate(False)
+            e.next_iter()
+            done += 1
+            e.set_iteration(done)  # the driver sets the round, as bfs.cu:98-108 does
+        e.get_results()
+    assert np.array_equal(vd, ref) and done == st["iterations"]

@@ -90,7 +90,7 @@ struct Ctl {
   ListCtl f[2];  // frontier lists
   ListCtl s[2];  // scatter lists
   unsigned tile[2];
-  unsigned bar[2];  // persistent-kernel grid barrier: arrivals, generation
+  unsigned bar[2];  // persistent-kernel grid barrier: arrival word, unused
   int32_t rounds;   // rounds executed by the last persistent run
   int32_t vcur;     // 1 when that run's result is in the alternate buffer
   int32_t denseEnd; // 1 when that run stopped before a dense round (gas_run_args::denseEndOut)
@@ -138,7 +138,9 @@ struct gas_core_s {
   int32_t *inOff = nullptr, *inSrc = nullptr, *outOff = nullptr, *outDst = nullptr;
   void *ed = nullptr;
   void *vd = nullptr, *vnew = nullptr, *vsaved = nullptr, *valt = nullptr;
-  int32_t *retStamp[2] = {nullptr, nullptr};
+  uint32_t *retBits = nullptr;  // three frontier bitmaps of bitWords words
+  uint32_t *frontBits = nullptr;  // three active-set bitmaps of the fused rounds
+  int32_t bitWords = 0;
   // degree bins of the dense pass (see dense.cuh)
   int32_t *binMid = nullptr, *binSmall = nullptr, *binTiny = nullptr;
   int32_t nMid = 0, nSmall = 0, nTiny = 0;
@@ -170,12 +172,11 @@ struct gas_core_s {
   bool countValid = false;
   int32_t countCache = 0;
   // A persistent run that stopped at maxIters before a dense round leaves
-  // its next frontier as the vertices stamped densePendStamp in
-  // retStamp[densePendArr]; materialize() turns it into a list when a later
+  // its next frontier as the bits of the round densePendStamp (bitmap
+  // densePendStamp % 3); materialize() turns it into a list when a later
   // call needs one.
   bool densePending = false;
   int32_t densePendStamp = 0;
-  int densePendArr = 0;
   unsigned dirty = 0;
   unsigned epoch = 0;
   int32_t stamp = 0;
@@ -193,11 +194,17 @@ struct gas_core_s {
   int32_t gatherLaunches = 0, scatterLaunches = 0;
 };
 
+// The frontier bitmap of the round with this stamp (three rotate, see
+// gas_run_args::retBits).
+static uint32_t *round_bits(gas_core_s *c, int32_t stamp) {
+  return c->retBits + (size_t)((unsigned)stamp % 3u) * c->bitWords;
+}
+
 namespace {
 
 void free_graph(gas_core *c) {
   void *ptrs[] = {c->inOff, c->inSrc, c->outOff, c->outDst, c->ed, c->vd, c->vnew, c->vsaved,
-                  c->valt, c->retStamp[0], c->retStamp[1], c->binMid, c->binSmall,
+                  c->valt, c->retBits, c->frontBits, c->binMid, c->binSmall,
                   c->binTiny, c->chunkVertex, c->chunkBegin, c->chunkFirst, c->chunkCount,
                   c->chunkSlot, c->chunkArrive, c->chunkFlags, c->chunkVal,
                   c->fvid[0], c->fvid[1], c->fpre[0], c->fpre[1], c->fsplit[0], c->fsplit[1],
@@ -212,7 +219,8 @@ void free_graph(gas_core *c) {
   c->fcell = nullptr;
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
-  c->retStamp[0] = c->retStamp[1] = nullptr;
+  c->retBits = nullptr;
+  c->frontBits = nullptr;
   c->binMid = c->binSmall = c->binTiny = nullptr;
   c->chunkVertex = c->chunkBegin = c->chunkFirst = c->chunkCount = c->chunkSlot = nullptr;
   c->chunkArrive = c->chunkFlags = nullptr;
@@ -290,7 +298,7 @@ gas_status materialize(gas_core *c) {
   gas_status st = clean(c, sbit(c->sidx) | fbit(c->cur) | kT0 | kT1);
   if (st) return st;
   gas::detail::compact_ret_kernel<<<c->scatterGrid, 256, 0, c->stream>>>(
-      c->retStamp[c->densePendArr], c->densePendStamp, c->outOff, c->nV, scat_list(c, c->sidx),
+      round_bits(c, c->densePendStamp), c->outOff, c->nV, scat_list(c, c->sidx),
       c->maxScatTiles, &c->ctl->err);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "frontier compaction launch");
@@ -514,10 +522,12 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
     if (e == cudaSuccess) e = r;
   };
   A(dalloc(&c->inOff, (size_t)nV + 1));
-  A(dalloc(&c->inSrc, (size_t)nE));
+  // whole 16-byte quads: the dense pass reads source ids (and 4-byte edge
+  // data) four at a time, up to the quad that holds a vertex's last edge
+  A(dalloc(&c->inSrc, (size_t)nE + 4));
   A(dalloc(&c->outOff, (size_t)nV + 1));
   A(dalloc(&c->outDst, (size_t)nE));
-  if (edgeBytes > 0) A(cudaMalloc(&c->ed, (size_t)edgeBytes * std::max(nE, 1)));
+  if (edgeBytes > 0) A(cudaMalloc(&c->ed, (size_t)edgeBytes * ((size_t)nE + 4)));
   if (edgeBytes > 0) A(dalloc(&c->cscPerm, (size_t)nE));
   const bool edgeMap = c->edgeScatterOn && edgeBytes > 0;
   if (c->keepCsrPerm || edgeMap) A(dalloc(&c->csrPerm, (size_t)nE));
@@ -556,16 +566,18 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   A(cudaMalloc(&c->vd, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->vnew, (size_t)vertexBytes * std::max(nV, 1)));
   A(cudaMalloc(&c->valt, (size_t)vertexBytes * std::max(nV, 1)));
-  A(dalloc(&c->retStamp[0], (size_t)nV));
-  A(dalloc(&c->retStamp[1], (size_t)nV));
+  c->bitWords = (nV + 31) / 32;
+  A(dalloc(&c->retBits, 3 * (size_t)c->bitWords));
   c->maxInDeg = 0;
   c->maxOutDeg = 0;
   for (int32_t v = 0; v < nV; ++v) {
     c->maxInDeg = std::max(c->maxInDeg, c->hInOff[(size_t)v + 1] - c->hInOff[v]);
     c->maxOutDeg = std::max(c->maxOutDeg, c->hOutOff[(size_t)v + 1] - c->hOutOff[v]);
   }
-  if (c->maxInDeg <= GAS_TPV_MAX_DEGREE && c->maxOutDeg <= GAS_TPV_MAX_DEGREE)  // fused rounds
+  if (c->maxInDeg <= GAS_TPV_MAX_DEGREE && c->maxOutDeg <= GAS_TPV_MAX_DEGREE) {  // fused rounds
     A(cudaMalloc(&c->fcell, (size_t)GAS_FUSED_CELL_BYTES(vertexBytes) * std::max(nV, 1)));
+    A(dalloc(&c->frontBits, 3 * (size_t)c->bitWords));
+  }
   // in-degree bins of the dense pass
   std::vector<int32_t> bMid, bSmall, bTiny, chV, chB, chF, chC, chS;
   for (int32_t v = 0; v < nV; ++v) {
@@ -632,8 +644,9 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
     return cuda_fail(e, "setGraph device allocation");
   }
   A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
-  for (int k = 0; k < 2; ++k)
-    A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(nV, 1), c->stream));
+  A(cudaMemsetAsync(c->retBits, 0, sizeof(uint32_t) * 3 * std::max(c->bitWords, 1), c->stream));
+  if (c->frontBits)
+    A(cudaMemsetAsync(c->frontBits, 0, sizeof(uint32_t) * 3 * std::max(c->bitWords, 1), c->stream));
   auto up = [&](int32_t *dst, const std::vector<int32_t> &src) {
     if (!src.empty())
       A(cudaMemcpyAsync(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice,
@@ -1008,8 +1021,9 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   }
   if (c->stamp > 0x40000000) {
     A(cudaMemsetAsync(c->mark, 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
-    for (int k = 0; k < 2; ++k)
-      A(cudaMemsetAsync(c->retStamp[k], 0, sizeof(int32_t) * std::max(c->nV, 1), c->stream));
+    A(cudaMemsetAsync(c->retBits, 0, sizeof(uint32_t) * 3 * std::max(c->bitWords, 1), c->stream));
+  if (c->frontBits)
+    A(cudaMemsetAsync(c->frontBits, 0, sizeof(uint32_t) * 3 * std::max(c->bitWords, 1), c->stream));
     c->stamp = 0;
   }
   A(cudaMemsetAsync(&c->ctl->dense[0][0], 0, sizeof(c->ctl->dense), c->stream));
@@ -1061,8 +1075,19 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.barrier = &c->ctl->bar[0];
   ra.roundsOut = &c->ctl->rounds;
   ra.vertexAlt = c->valt;
-  ra.retStamp[0] = c->retStamp[0];
-  ra.retStamp[1] = c->retStamp[1];
+  for (int k = 0; k < 3; ++k) {
+    ra.retBits[k] = c->retBits + (size_t)k * c->bitWords;
+    ra.frontBits[k] = c->frontBits ? c->frontBits + (size_t)k * c->bitWords : nullptr;
+  }
+  ra.bitWords = c->bitWords;
+  // round 0 writes the bitmap of stamp stampBase: clear at launch (each round
+  // clears the one after it)
+  A(cudaMemsetAsync(round_bits(c, ra.stampBase), 0, sizeof(uint32_t) * std::max(c->bitWords, 1),
+                    c->stream));
+  // and a fused round 0 writes the active-set bitmap of stampBase + 1
+  if (c->frontBits)
+    A(cudaMemsetAsync(c->frontBits + (size_t)((unsigned)(ra.stampBase + 1) % 3u) * c->bitWords, 0,
+                      sizeof(uint32_t) * std::max(c->bitWords, 1), c->stream));
   ra.binMid = c->binMid;
   ra.binSmall = c->binSmall;
   ra.binTiny = c->binTiny;
@@ -1132,7 +1157,6 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   if (rv[2] && R > 0) {  // the next frontier is the last round's stamps
     c->densePending = true;
     c->densePendStamp = c->stamp;  // the last round's stamp
-    c->densePendArr = (R - 1) & 1;
   }
   if (iterations) *iterations = R;
   return check_device_error(c);
