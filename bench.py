@@ -733,6 +733,8 @@ def measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu=True):
         for _ in range(steps):
             batched_step()
     head = [i for i, x in enumerate(sets) if x[3] != 5]   # BFS + SSSP: the metric's queries
+    if not head:  # a subset of PPR sets only (--c4-sets): report those
+        head = list(range(len(sets)))
     total_ms = allreduce_max(world, float(sum(per_set_ms[i] for i in head)))
     queries = allreduce_sum(world, float(len(head) * nq * steps))
     value = queries / (total_ms / 1e3)

@@ -40,6 +40,7 @@ constexpr int kPprRounds = 20;    // PPR iterations (a fixed count, as run(20))
 constexpr int kFirstChunk = 4;    // rounds queued per chunk: 4, 8, ... 64
 constexpr int kMaxChunk = 64;
 constexpr int kKinds = 3;         // BFS, SSSP, PPR
+constexpr int kMaxPersistent = 2; // batches in a cooperative launch at once, a third of the device each
 constexpr int64_t kTieNs = 20000000;  // queries this close in arrival count as a burst
 constexpr int64_t kWindowDiv = 32;         // batching window: recent run time / kWindowDiv
 constexpr int64_t kWindowMaxNs = 10000000;
@@ -123,6 +124,7 @@ struct Batch {
   gas::detail::BatchArgs ba;
   gas::detail::PprArgs pa;
   bool pairs = false;             // (vertex, query) pair frontier
+  bool persistent = false;        // every round in one cooperative launch
   int64_t pairsSeen = 0;          // largest pair list seen at a chunk's end
   int32_t delta = 0;              // SSSP distance buckets
   int roundsIssued = 0;
@@ -176,6 +178,7 @@ class Server {
   gas_server_stats stats;
   std::atomic<int64_t> bytesInUse{0};
   std::atomic<int64_t> launches{0};  // kernels launched (scheduler thread)
+  int persistentRunning = 0;         // batches in a cooperative launch (scheduler thread)
   std::thread sched;
   bool stop = false;
 
@@ -344,6 +347,22 @@ void ppr_start_launch(const gas::detail::PprArgs &a, int blocks, cudaStream_t s)
     case 128: FN<128>(__VA_ARGS__); break;        \
     default: FN<256>(__VA_ARGS__); break;         \
   }
+
+// The batch engine's persistent kernel for a batch's row width and program.
+const void *batch_run_fn(int W, bool bfs) {
+#define GAS_RUN_W(w)                                                                       \
+  case w:                                                                                  \
+    return bfs ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS>    \
+               : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP>;
+  switch (W) {
+    GAS_RUN_W(1)
+    GAS_RUN_W(2)
+    GAS_RUN_W(4)
+    default:
+      GAS_RUN_W(8)
+  }
+#undef GAS_RUN_W
+}
 
 void enqueue_round(Batch &b, int r, int blocks) {
   unsigned *done = &b.ctl->done;
@@ -526,6 +545,30 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch start");
   L.batch = bp;
+  if (b.kind != 2 && b.pairs && persistentRunning < kMaxPersistent) {
+    // A pair-frontier batch (lattice-like graph: thousands of small rounds)
+    // runs every round in one cooperative launch of the batch engine's
+    // kernel on its lane's high-priority stream, on a third of the device's
+    // co-resident blocks: its rounds then no longer queue behind other
+    // lanes' launches.  At most kMaxPersistent such batches run at once, so
+    // their grids fit the device together; the other lanes' kernels are
+    // ordinary and finite, so a partly placed grid waits for their blocks
+    // to finish, and every grid-barrier wait in it is bounded.
+    const void *fn = batch_run_fn(b.W, b.kind == 0);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
+    const int blocks = std::max(1, per * sms / 3);
+    void *args[] = {&b.ba};
+    e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(256), args, 0, b.stream);
+    if (e == cudaSuccess) {
+      b.persistent = true;
+      ++persistentRunning;
+      launches += 1;
+      issue_chunk(l, 0, true);
+      return GAS_OK;
+    }
+    cudaGetLastError();  // cannot launch cooperatively: round by round below
+  }
   if (b.kind == 2) {
     issue_chunk(l, kPprRounds, false);
     issue_chunk(l, 0, true);
@@ -544,6 +587,10 @@ void Server::finish_batch(int l, gas_status st, int32_t rounds) {
   Lane &L = lanes[l];
   std::shared_ptr<Batch> bp = L.batch;
   Batch &b = *bp;
+  if (b.persistent) {
+    --persistentRunning;
+    b.persistent = false;
+  }
   if (b.state) {
     cudaFreeAsync(b.state, b.stream);
     bytesInUse -= b.stateBytes;
