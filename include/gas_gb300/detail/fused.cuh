@@ -52,6 +52,10 @@ struct FusedCtx {
   void *vd;             // the run's vertex data (apply-only Programs update it in place)
   uint32_t stamp;       // this round's stamp
   uint32_t *nextBits;   // the next round's frontier bitmap (activated vertices)
+  const int32_t *ellIn;   // [V][width] in-neighbours, -1 after the last
+  const int32_t *ellOut;  // [V][width] out-neighbours, -1 after the last
+  const void *ellEd;      // [V][width] edge data of the in-edges
+  int32_t width;          // 4 or 8
 };
 
 // A fused round's counts, added once per block.
@@ -97,68 +101,131 @@ __device__ void fused_enter(const FusedCtx &f, const void *vd, int nVertices) {
   }
 }
 
-// Vertex v (in-degree deg from CSC position beg; deg < 0: read from the
-// CSC offsets) in a fused round: gather from the in-neighbours' cells,
-// apply, write the cell, and when apply returns true set the out-
-// neighbours' bits in the next frontier.
-template <class P>
-__device__ __forceinline__ void fused_vertex(const gas_gather_args &a, const ScatterArgs &sa,
-                                             const FusedCtx &f, int v, int beg, int deg,
-                                             FusedCounts &c) {
+// Row v of a fixed-width adjacency: W int32 as W / 4 16-byte loads.
+template <int W>
+__device__ __forceinline__ void load_row(const int32_t *rows, int v, int32_t (&out)[W]) {
+  const int4 *p = reinterpret_cast<const int4 *>(rows) + (size_t)v * (W / 4);
+#pragma unroll
+  for (int q = 0; q < W / 4; ++q) {
+    const int4 t = __ldg(p + q);
+    out[4 * q] = t.x;
+    out[4 * q + 1] = t.y;
+    out[4 * q + 2] = t.z;
+    out[4 * q + 3] = t.w;
+  }
+}
+
+// Vertices vs[0..K) (vs[k] < 0: none) in a fused round, their loads
+// interleaved: each gathers from its in-neighbours' cells, applies, writes
+// its cell, and when apply returns true sets its out-neighbours' bits in the
+// next frontier.  Rows of width W (fixed-width adjacency).
+template <class P, int K, int W>
+__device__ __forceinline__ void fused_vertices(const gas_gather_args &a, const FusedCtx &f,
+                                               const int (&vs)[K], FusedCounts &c) {
   typedef typename P::VertexData VD;
   typedef typename P::GatherResult GR;
-  constexpr int D = GAS_TPV_MAX_DEGREE;
-  if (deg < 0) {
-    beg = a.inOffsets[v];
-    deg = a.inOffsets[v + 1] - beg;
+  typedef typename P::EdgeData ED;
+  constexpr bool kQuadEd = !std::is_empty<ED>::value && sizeof(ED) == 4;
+  int32_t outd[K][W], src[K][W];
+  int32_t edw[K][kQuadEd ? W : 1];
+  FusedCell<VD> cv[K];
+  VD tmp[K];
+  // one round trip: the rows and the vertex's own cell
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int v = vs[k] < 0 ? 0 : vs[k];
+    if (vs[k] >= 0) {
+      load_row<W>(f.ellOut, v, outd[k]);
+      if (a.haveGather) {
+        load_row<W>(f.ellIn, v, src[k]);
+        if constexpr (kQuadEd) load_row<W>(reinterpret_cast<const int32_t *>(f.ellEd), v, edw[k]);
+        cv[k] = load_cell(reinterpret_cast<const FusedCell<VD> *>(f.cells) + v);
+      } else {
+        tmp[k] = reinterpret_cast<const VD *>(f.vd)[v];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < W; ++j) outd[k][j] = src[k][j] = -1;
+    }
   }
-  const int obeg = a.outOffsets[v], oend = a.outOffsets[v + 1];
-  FusedCell<VD> *cell = reinterpret_cast<FusedCell<VD> *>(f.cells) + v;
-  int own = 0;
-  VD tmp;
   if (a.haveGather) {
-    const FusedCell<VD> cv = load_cell(cell);
-    own = (int)(cv.ver & 1u);  // v is applied once per round: its word is still old
-    tmp = own ? cv.s[1] : cv.s[0];
-  } else {
-    tmp = reinterpret_cast<const VD *>(f.vd)[v];
-  }
-  // out-neighbours loaded before apply decides whether they are activated
-  const int odeg = oend - obeg;
-  int32_t outd[D];
+    // second round trip: the in-neighbours' cells
+    VD sv[K][W];
 #pragma unroll
-  for (int k = 0; k < D; ++k) outd[k] = k < odeg ? __ldg(sa.outDests + obeg + k) : 0;
-  bool r;
-  if (a.haveGather) {
-    int src[D];
+    for (int k = 0; k < K; ++k)
 #pragma unroll
-    for (int k = 0; k < D; ++k) src[k] = k < deg ? __ldg(a.inSources + beg + k) : 0;
-    VD sv[D];
+      for (int j = 0; j < W; ++j)
+        if (src[k][j] >= 0) sv[k][j] = fused_read<VD>(f, src[k][j]);
 #pragma unroll
-    for (int k = 0; k < D; ++k)
-      if (k < deg) sv[k] = fused_read<VD>(f, src[k]);
-    GR acc = P::gatherZero;
+    for (int k = 0; k < K; ++k) {
+      if (vs[k] < 0) continue;
+      const int own = (int)(cv[k].ver & 1u);  // v is applied once per round: its word is still old
+      VD t = own ? cv[k].s[1] : cv[k].s[0];
+      GR acc = P::gatherZero;
+      unsigned deg = 0u;
 #pragma unroll
-    for (int k = 0; k < D; ++k)
-      if (k < deg)
-        acc = P::gatherReduce(acc, P::gatherMap(&tmp, &sv[k], edge_ptr<P>(a.edgeData, beg + k)));
-    r = do_apply<P>(&tmp, acc, a.iteration);
-    cell->s[own ^ 1] = tmp;
-    cell->ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
+      for (int j = 0; j < W; ++j)
+        if (src[k][j] >= 0) {
+          const ED *ep;
+          ED e;
+          if constexpr (kQuadEd) {
+            memcpy(&e, &edw[k][j], sizeof(ED));
+            ep = &e;
+          } else if constexpr (std::is_empty<ED>::value) {
+            ep = nullptr;
+          } else {
+            ep = reinterpret_cast<const ED *>(f.ellEd) + (size_t)vs[k] * W + j;
+          }
+          acc = P::gatherReduce(acc, P::gatherMap(&t, &sv[k][j], ep));
+          ++deg;
+        }
+      const bool r = do_apply<P>(&t, acc, a.iteration);
+      FusedCell<VD> *cell = reinterpret_cast<FusedCell<VD> *>(f.cells) + vs[k];
+      cell->s[own ^ 1] = t;
+      cell->ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
+      ++c.active;
+      c.inEdges += deg;
+      if (r) {
+        ++c.ret;
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          if (outd[k][j] >= 0) {
+            bit_set(f.nextBits, outd[k][j]);
+            ++c.outEdges;
+          }
+      }
+    }
   } else {  // apply only: nothing reads other vertices, update in place
-    const GR gz = P::gatherZero;
-    r = do_apply<P>(&tmp, gz, a.iteration);
-    reinterpret_cast<VD *>(f.vd)[v] = tmp;
-  }
-  ++c.active;
-  c.inEdges += (unsigned)deg;
-  if (r) {
-    ++c.ret;
-    c.outEdges += (unsigned)odeg;
 #pragma unroll
-    for (int k = 0; k < D; ++k)
-      if (k < odeg) bit_set(f.nextBits, outd[k]);
+    for (int k = 0; k < K; ++k) {
+      if (vs[k] < 0) continue;
+      const GR gz = P::gatherZero;
+      const bool r = do_apply<P>(&tmp[k], gz, a.iteration);
+      reinterpret_cast<VD *>(f.vd)[vs[k]] = tmp[k];
+      ++c.active;
+      c.inEdges += (unsigned)(a.inOffsets[vs[k] + 1] - a.inOffsets[vs[k]]);
+      if (r) {
+        ++c.ret;
+#pragma unroll
+        for (int j = 0; j < W; ++j)
+          if (outd[k][j] >= 0) {
+            bit_set(f.nextBits, outd[k][j]);
+            ++c.outEdges;
+          }
+      }
+    }
   }
+}
+
+// One vertex (width from the context).
+template <class P>
+__device__ __forceinline__ void fused_vertex(const gas_gather_args &a, const FusedCtx &f, int v,
+                                             FusedCounts &c) {
+  const int vs[1] = {v};
+  if (f.width == 4)
+    fused_vertices<P, 1, 4>(a, f, vs, c);
+  else
+    fused_vertices<P, 1, 8>(a, f, vs, c);
 }
 
 // A fused round whose frontier is a list (or the range of setActive): the
@@ -173,7 +240,7 @@ __device__ __forceinline__ void fused_list_round(const gas_gather_args &a, const
     if (i < n) {
       int v, pre, end, beg;
       front_entry(a, i, n, T, v, pre, end, beg);
-      fused_vertex<P>(a, sa, f, v, beg, end - pre, c);
+      fused_vertex<P>(a, f, v, c);
     }
   }
 }
@@ -212,7 +279,14 @@ __device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const
       sm.vid[off++] = w * 32 + b;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < (int)total; i += NT) fused_vertex<P>(a, sa, f, sm.vid[i], 0, -1, c);
+    if (f.width == 4) {  // two listed vertices a thread, their loads interleaved
+      for (int i = threadIdx.x; i < (int)total; i += 2 * NT) {
+        const int vs[2] = {sm.vid[i], i + NT < (int)total ? sm.vid[i + NT] : -1};
+        fused_vertices<P, 2, 4>(a, f, vs, c);
+      }
+    } else {
+      for (int i = threadIdx.x; i < (int)total; i += NT) fused_vertex<P>(a, f, sm.vid[i], c);
+    }
     __syncthreads();  // sm.vid is rewritten by the next pass
   }
 }

@@ -354,6 +354,10 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         f.vd = vdBuf[vcur];
         f.stamp = (uint32_t)stamp;
         f.nextBits = front_bits(ra, stamp + 1);
+        f.ellIn = ra.ellIn;
+        f.ellOut = ra.ellOut;
+        f.ellEd = ra.ellEd;
+        f.width = ra.ellWidth;
         if (a.haveGather && !versioned) {  // the vertex data moves into the cells
           fused_enter<P>(f, vdBuf[vcur], a.nVertices);
           versioned = true;

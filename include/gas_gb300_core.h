@@ -163,6 +163,14 @@ typedef struct {
   /* fused list rounds (every degree <= 8): gather, apply and activation in
    * one phase, vertex data versioned across the two buffers */
   int32_t fused;
+  /* fixed-width adjacency rows of fused graphs (every degree <= 8): row v of
+   * ellWidth entries (4 or 8) holds v's in-neighbours (ellIn, CSC order, -1
+   * after the last), their edge data (ellEd, edgeBytes each) and v's
+   * out-neighbours (ellOut, -1 after the last) */
+  const int32_t *ellIn;
+  const int32_t *ellOut;
+  const void *ellEd;
+  int32_t ellWidth;
   void *fusedCells;           /* [V] cells of GAS_FUSED_CELL_BYTES(vertexBytes) each:
                                  two value slots and (stamp << 1) | newest slot */
   /* the run starts with dense rounds (allActive): the caller may run them in

@@ -116,6 +116,25 @@ cudaError_t dalloc(T **p, size_t count) {
 
 }  // namespace
 
+// Fixed-width rows of an adjacency (offsets, indices; optional per-edge
+// bytes): row v holds v's first `width` indices in order, -1 after the last
+// (zero bytes for the edge data there).
+__global__ void ell_rows_kernel(int32_t nV, const int32_t *off, const int32_t *idx, const void *ed,
+                                int32_t edgeBytes, int32_t width, int32_t *rows, void *edRows) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nV;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t b = off[v], d = off[v + 1] - b;
+    for (int k = 0; k < width; ++k) {
+      rows[v * width + k] = k < d ? idx[b + k] : -1;
+      if (edRows) {
+        unsigned char *dst = static_cast<unsigned char *>(edRows) + (v * width + k) * edgeBytes;
+        const unsigned char *src = static_cast<const unsigned char *>(ed) + (int64_t)(b + k) * edgeBytes;
+        for (int32_t x = 0; x < edgeBytes; ++x) dst[x] = k < d ? src[x] : 0;
+      }
+    }
+  }
+}
+
 struct gas_core_s {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -131,6 +150,9 @@ struct gas_core_s {
   bool keepCsrPerm = false;
   int32_t *csr2csc = nullptr;   // [E] CSC position of each CSR edge (Program::scatter)
   void *fcell = nullptr;        // [V] cells of fused rounds (fused.cuh), fused-eligible graphs only
+  int32_t *ellIn = nullptr, *ellOut = nullptr;  // fixed-width adjacency rows (fused graphs)
+  void *ellEd = nullptr;
+  int32_t ellWidth = 0;
   int32_t maxOutDeg = 0;
   bool fusedRounds = true;      // one-phase rounds when every degree is <= 8
   bool edgeScatterOn = false;   // keep csr2csc and run scatter-capable rounds
@@ -211,12 +233,15 @@ void free_graph(gas_core *c) {
                   c->fbeg[0], c->fbeg[1], c->sbeg[0], c->sbeg[1],
                   c->rsplit, c->svid[0], c->svid[1], c->spre[0], c->spre[1], c->ssplit[0],
                   c->ssplit[1], c->mark, c->carryVal, c->carryFlag, c->ctl, c->stats,
-                  c->cscPerm, c->csrPerm, c->csr2csc, c->fcell};
+                  c->cscPerm, c->csrPerm, c->csr2csc, c->fcell, c->ellIn, c->ellOut, c->ellEd};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->cscPerm = c->csrPerm = nullptr;
   c->csr2csc = nullptr;
   c->fcell = nullptr;
+  c->ellIn = c->ellOut = nullptr;
+  c->ellEd = nullptr;
+  c->ellWidth = 0;
   c->inOff = c->inSrc = c->outOff = c->outDst = nullptr;
   c->ed = c->vd = c->vnew = c->vsaved = c->valt = nullptr;
   c->retBits = nullptr;
@@ -576,6 +601,21 @@ gas_status gas_core_set_graph(gas_core *c, int32_t nV, int32_t nE, const int32_t
   }
   if (c->maxInDeg <= GAS_TPV_MAX_DEGREE && c->maxOutDeg <= GAS_TPV_MAX_DEGREE) {  // fused rounds
     A(cudaMalloc(&c->fcell, (size_t)GAS_FUSED_CELL_BYTES(vertexBytes) * std::max(nV, 1)));
+    // fixed-width adjacency rows: a vertex's neighbours in one or two 16-byte
+    // loads addressed by its id, no offset lookup
+    c->ellWidth = std::max(c->maxInDeg, c->maxOutDeg) <= 4 ? 4 : 8;
+    const size_t cells = (size_t)std::max(nV, 1) * c->ellWidth;
+    A(dalloc(&c->ellIn, cells));
+    A(dalloc(&c->ellOut, cells));
+    if (edgeBytes > 0) A(cudaMalloc(&c->ellEd, cells * edgeBytes));
+    if (e == cudaSuccess && nV > 0) {
+      const int blocks = (int)std::min<int64_t>(((int64_t)nV + 255) / 256, 65535LL * 32);
+      ell_rows_kernel<<<blocks, 256, 0, c->stream>>>(nV, c->inOff, c->inSrc, c->ed, edgeBytes,
+                                                     c->ellWidth, c->ellIn, c->ellEd);
+      ell_rows_kernel<<<blocks, 256, 0, c->stream>>>(nV, c->outOff, c->outDst, nullptr, 0,
+                                                     c->ellWidth, c->ellOut, nullptr);
+      A(cudaGetLastError());
+    }
     A(dalloc(&c->frontBits, 3 * (size_t)c->bitWords));
   }
   // in-degree bins of the dense pass
@@ -1106,6 +1146,10 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
   ra.chunkFlags = c->chunkFlags;
   ra.denseCnt = &c->ctl->dense[0][0];
   ra.fusedCells = c->fcell;
+  ra.ellIn = c->ellIn;
+  ra.ellOut = c->ellOut;
+  ra.ellEd = c->ellEd;
+  ra.ellWidth = c->ellWidth;
   ra.fused = (c->fcell && c->fusedRounds && !c->csr2csc && c->maxInDeg <= GAS_TPV_MAX_DEGREE &&
               c->maxOutDeg <= GAS_TPV_MAX_DEGREE)
                  ? 1
