@@ -387,6 +387,32 @@ __device__ __forceinline__ void warp_append_pair(bool want, uint32_t entry, uint
   if (want) list[base + __popc(who & ((1u << lane) - 1u))] = entry;
 }
 
+// Appends each lane's entries out[k] with want[k] (k < K) to a pair list:
+// one atomic per warp for all K.  Warp-uniform call.
+template <int K>
+__device__ __forceinline__ void warp_append_pairs(const bool (&want)[K], const uint32_t (&out)[K],
+                                                  uint32_t *list, unsigned long long *cnt) {
+  const int lane = threadIdx.x & 31;
+  unsigned n = 0u;
+#pragma unroll
+  for (int k = 0; k < K; ++k) n += want[k] ? 1u : 0u;
+  unsigned incl = n;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned o = __shfl_up_sync(kFullMask, incl, d);
+    if (lane >= d) incl += o;
+  }
+  const unsigned total = __shfl_sync(kFullMask, incl, 31);
+  if (total == 0u) return;
+  unsigned long long base = 0ull;
+  if (lane == 31) base = atomicAdd(cnt, (unsigned long long)total << 32);
+  base = __shfl_sync(kFullMask, base, 31) >> 32;
+  unsigned long long pos = base + (incl - n);
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (want[k]) list[pos++] = out[k];
+}
+
 // Pair-frontier push: lane i takes entry i of the current pair list (when
 // `valid`), a changed (u, q), and relaxes u's out-edges for q alone; a
 // destination whose value changes is appended as (v, q) the first time its
@@ -423,33 +449,42 @@ __device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, 
     }
   }
   if (KIND == kBatchSSSP && bk.bound) warp_append_pair(keep, entry, listNext, cntNext);
+  // four out-edges a step, their appends to the next list in one atomic per
+  // warp (the list counter is one word every warp of the grid contends for)
+  constexpr int J = 4;
   const int maxDeg = __reduce_max_sync(kFullMask, deg);
-  for (int j = 0; j < maxDeg; ++j) {
-    bool want = false;
-    uint32_t out = 0u;
-    if (j < deg) {
-      const int v = __ldg(a.outDests + eb + j);
-      if (KIND == kBatchBFS) {
-        const unsigned old = atomicOr(a.seen + (size_t)v * W + wq, bit);
-        if (!(old & bit)) {
-          a.value[(size_t)v * Q + q] = round + 1;
-          want = true;
+  for (int j0 = 0; j0 < maxDeg; j0 += J) {
+    bool want[J];
+    uint32_t out[J];
+#pragma unroll
+    for (int t = 0; t < J; ++t) {
+      const int j = j0 + t;
+      want[t] = false;
+      out[t] = 0u;
+      if (j < deg) {
+        const int v = __ldg(a.outDests + eb + j);
+        if (KIND == kBatchBFS) {
+          const unsigned old = atomicOr(a.seen + (size_t)v * W + wq, bit);
+          if (!(old & bit)) {
+            a.value[(size_t)v * Q + q] = round + 1;
+            want[t] = true;
+          }
+        } else {
+          const int cand = du + __ldg(a.weightsOut + eb + j);
+          const int old = atomicMin(a.value + (size_t)v * Q + q, cand);
+          if (cand < old) {
+            const unsigned o2 = atomicOr(nxt + (size_t)v * W + wq, bit);
+            want[t] = !(o2 & bit);
+            if (bk.bound && cand < bk.bound[q] && !(bk.near[wq] & bit)) atomicOr(bk.near + wq, bit);
+          }
         }
-      } else {
-        const int cand = du + __ldg(a.weightsOut + eb + j);
-        const int old = atomicMin(a.value + (size_t)v * Q + q, cand);
-        if (cand < old) {
-          const unsigned o2 = atomicOr(nxt + (size_t)v * W + wq, bit);
-          want = !(o2 & bit);
-          if (bk.bound && cand < bk.bound[q] && !(bk.near[wq] & bit)) atomicOr(bk.near + wq, bit);
+        if (want[t]) {
+          changed += 1;
+          out[t] = ((uint32_t)v << LOGQ) | (uint32_t)q;
         }
-      }
-      if (want) {
-        changed += 1;
-        out = ((uint32_t)v << LOGQ) | (uint32_t)q;
       }
     }
-    warp_append_pair(want, out, listNext, cntNext);
+    warp_append_pairs<J>(want, out, listNext, cntNext);
   }
 }
 
@@ -474,8 +509,12 @@ __device__ __forceinline__ void batch_compact(const BatchArgs &a, const unsigned
   }
 }
 
-template <int W, int KIND>
-__global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
+// PAIRS: the instantiation for pair-frontier batches (a.pairMode set),
+// which holds only the pair rounds: its smaller register budget (at most 64
+// a thread) keeps more warps, and so more of the latency-bound atomics, in
+// flight.  The other instantiation serves vertex-mask batches.
+template <int W, int KIND, bool PAIRS = false>
+__global__ void __launch_bounds__(256, PAIRS ? 6 : 1) batch_run_kernel(const BatchArgs a) {
   __shared__ int32_t sBound[32 * W];
   __shared__ unsigned sNear[W];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);
@@ -522,12 +561,12 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       a.cnt[rn] = 0ull;
       a.listCnt[(r + 2) % 3] = 0ull;  // input of round r-1, appended in round r+1
     }
-    if (!a.pairMode)  // pair rounds clear their own mask words (batch_pair_unit)
+    if (!PAIRS)  // pair rounds clear their own mask words (batch_pair_unit)
       for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < maskWords;
            i += (size_t)gridDim.x * blockDim.x)
         clr[i] = 0u;
     unsigned long long changed = 0ull;
-    if (a.pairMode) {
+    if constexpr (PAIRS) {
       const uint32_t *pc = a.pairs[rc];
       uint32_t *pn = a.pairs[rn];
       const long long threads = (long long)gridDim.x * blockDim.x;
@@ -545,6 +584,7 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
       for (long long u = gw; u < a.nUnits; u += warps)
         batch_unit<W, KIND>(a, (int)u, r, cur, nxt, changed);
     }
+    (void)clr;
     changed = warp_sum_u64(changed);
     if ((threadIdx.x & 31) == 0 && changed) atomicAdd(a.cnt + rc, changed);
     if (buckets) {
@@ -553,7 +593,7 @@ __global__ void __launch_bounds__(256) batch_run_kernel(const BatchArgs a) {
     }
     if (!grid_barrier(a.barrier, a.errWord)) break;
     if (a.cnt[rc] == 0ull) break;  // uniform: read after the barrier
-    if (!push) {
+    if (!PAIRS && !push) {
       batch_compact<W>(a, nxt, listNext, listNextC, cntNext);
       if (!grid_barrier(a.barrier, a.errWord)) break;
     }

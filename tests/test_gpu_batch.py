@@ -59,7 +59,7 @@ def test_batch_autotune_and_errors(gpu):
     with GASBatch() as b:
         b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights)
         chunk, blocks = b.autotune(PROGRAM_SSSP, 64)
-        assert chunk in (32, 128, 512, 2048) and blocks in (0, 1, 2)
+        assert chunk in (32, 128, 512, 2048) and blocks in (0, 1, 2, 4)
         with pytest.raises(GasError):
             b.run(PROGRAM_SSSP, np.array([g.n_vertices], np.int32))
         with pytest.raises(GasError):
@@ -157,7 +157,7 @@ def test_batch_ppr_hubs_equal_served(gpu, port):
         b.set_graph(g.n_vertices, g.srcs, g.dsts)
         b.autotune(PROGRAM_PPR, len(sources))
         t = b.tuning()
-        assert t["blocks_per_sm"] in (0, 1, 2)
+        assert t["blocks_per_sm"] in (0, 1, 2, 4)
         got, _ = b.run(PROGRAM_PPR, sources)
     with GASServer(lanes=2) as srv:
         gid = srv.add_graph(g.n_vertices, g.srcs, g.dsts)

@@ -252,8 +252,9 @@ gas_status launch_run(gas_batch *b, const CoreGraph &g, int32_t Q, int blocks, b
   a.pairMode = pairs ? 1 : 0;
   for (int k = 0; k < 3; ++k) a.pairs[k] = pairs ? b->pairs[k] : nullptr;
   void *args[] = {&a};
-  cudaError_t e = cudaLaunchCooperativeKernel((const void *)gas::detail::batch_run_kernel<W, KIND>,
-                                              dim3(blocks), dim3(256), args, 0, b->stream);
+  const void *fn = pairs ? (const void *)gas::detail::batch_run_kernel<W, KIND, true>
+                         : (const void *)gas::detail::batch_run_kernel<W, KIND, false>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(256), args, 0, b->stream);
   return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch run launch");
 }
 
@@ -265,14 +266,16 @@ gas_status launch_run_kind(gas_batch *b, const CoreGraph &g, int kind, int32_t Q
              : launch_run<W, gas::detail::kBatchSSSP>(b, g, Q, blocks, pairs);
 }
 
-int grid_blocks(gas_batch *b, int kind, int W) {
+int grid_blocks(gas_batch *b, int kind, int W, bool pairs) {
   int per = 0;
   const void *fn = nullptr;
-#define GAS_BATCH_FN(w)                                                                    \
-  if (W == w)                                                                              \
-    fn = kind == gas::detail::kBatchBFS                                                    \
-             ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS>      \
-             : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP>;
+#define GAS_BATCH_FN(w)                                                                       \
+  if (W == w)                                                                                 \
+    fn = kind == gas::detail::kBatchBFS                                                       \
+             ? (pairs ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS, true> \
+                      : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS, false>) \
+             : (pairs ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP, true> \
+                      : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP, false>);
   GAS_BATCH_FN(1) GAS_BATCH_FN(2) GAS_BATCH_FN(4) GAS_BATCH_FN(8)
 #undef GAS_BATCH_FN
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0);
@@ -304,7 +307,7 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
       b->list[0], b->listC[0], cv.listCnt, pairs ? b->pairs[0] : nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch init");
-  const int blocks = grid_blocks(b, kind, W);
+  const int blocks = grid_blocks(b, kind, W, pairs);
   gas_status st;
   switch (W) {
     case 1: st = launch_run_kind<1>(b, g, kind, Q, blocks, pairs); break;
@@ -812,7 +815,7 @@ gas_status gas_batch_autotune(gas_batch *b, int32_t program, int32_t nQueries,
     }
   }
   const int32_t chunks[] = {32, 128, 512, 2048};
-  const int32_t blocks[] = {0, 2, 1};
+  const int32_t blocks[] = {0, 4, 2, 1};
   float best = 1e30f;
   int32_t bc = b->chunk, bb = b->blocksPerSM;
   const int nc = program == GAS_PROGRAM_PPR ? 1 : 4;  // PPR's units are fixed (kPprChunk)

@@ -348,12 +348,13 @@ void ppr_start_launch(const gas::detail::PprArgs &a, int blocks, cudaStream_t s)
     default: FN<256>(__VA_ARGS__); break;         \
   }
 
-// The batch engine's persistent kernel for a batch's row width and program.
+// The batch engine's persistent kernel for a pair-frontier batch of a row
+// width and program.
 const void *batch_run_fn(int W, bool bfs) {
-#define GAS_RUN_W(w)                                                                       \
-  case w:                                                                                  \
-    return bfs ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS>    \
-               : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP>;
+#define GAS_RUN_W(w)                                                                             \
+  case w:                                                                                        \
+    return bfs ? (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchBFS, true>    \
+               : (const void *)gas::detail::batch_run_kernel<w, gas::detail::kBatchSSSP, true>;
   switch (W) {
     GAS_RUN_W(1)
     GAS_RUN_W(2)
