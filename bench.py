@@ -712,7 +712,7 @@ def measure_batch_c4(args, steps, warmup, world, rank, local, with_cpu=True):
             b = gas.GASBatch(device=local, stream=stream.cuda_stream)
             b.set_graph(g.n_vertices, g.srcs, g.dsts, g.weights if prog == 2 else None)
             if args.no_autotune:
-                b.set_config(256, 0, True)
+                b.set_config(256, args.c4_blocks, True)
                 b.set_delta(args.c4_delta if prog == 2 else 0)
             else:
                 b.autotune(prog, nq)
@@ -1174,6 +1174,8 @@ def main():
                     help="batch-c4: default launch configuration instead of the autotuner")
     ap.add_argument("--c4-delta", type=int, default=0,
                     help="batch-c4 with --no-autotune: SSSP bucket width")
+    ap.add_argument("--c4-blocks", type=int, default=0,
+                    help="batch-c4 with --no-autotune: CTAs per SM (0 = as many as fit)")
     ap.add_argument("--c5-lanes", type=int, default=C5_LANES,
                     help="serve-c5: batches in flight at once")
     ap.add_argument("--c5-graphs", default=None,

@@ -413,7 +413,10 @@ __device__ __forceinline__ void warp_append_pairs(const bool (&want)[K], const u
     if (want[k]) list[pos++] = out[k];
 }
 
-// Pair-frontier push: lane i takes entry i of the current pair list (when
+// Pair-frontier push (state query-major: value[q][v], mask and seen words
+// [w][v], so that the pairs of one query's wavefront, which relax
+// neighbouring vertices, touch neighbouring words): lane i takes entry i of
+// the current pair list (when
 // `valid`), a changed (u, q), and relaxes u's out-edges for q alone; a
 // destination whose value changes is appended as (v, q) the first time its
 // query bit is set this round.  Warp-uniform (lanes step through their
@@ -430,6 +433,7 @@ __device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, 
   const int q = (int)(entry & (Q - 1));
   const unsigned bit = 1u << (q & 31);
   const int wq = q >> 5;
+  const size_t V = (size_t)a.nVertices;  // pair batches keep their state query-major
   int eb = valid ? a.outOffsets[u] : 0;
   int deg = valid ? a.outOffsets[u + 1] - eb : 0;
   int du = 0;
@@ -439,10 +443,10 @@ __device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, 
     // list, and nothing else touches the mask this round: each pair clears
     // its word (idempotent zeros), so the mask is clean when it next
     // collects pairs, without a pass over all vertices.
-    cur[(size_t)u * W + wq] = 0u;
-    du = __ldcg(a.value + (size_t)u * Q + q);
+    cur[(size_t)wq * V + u] = 0u;
+    du = __ldcg(a.value + (size_t)q * V + u);
     if (bk.bound && du >= bk.bound[q]) {  // not this bucket: keep (u, q) for later
-      const unsigned old = atomicOr(nxt + (size_t)u * W + wq, bit);
+      const unsigned old = atomicOr(nxt + (size_t)wq * V + u, bit);
       keep = !(old & bit);
       changed += 1;
       deg = 0;
@@ -464,16 +468,16 @@ __device__ __forceinline__ void batch_pair_unit(const BatchArgs &a, bool valid, 
       if (j < deg) {
         const int v = __ldg(a.outDests + eb + j);
         if (KIND == kBatchBFS) {
-          const unsigned old = atomicOr(a.seen + (size_t)v * W + wq, bit);
+          const unsigned old = atomicOr(a.seen + (size_t)wq * V + v, bit);
           if (!(old & bit)) {
-            a.value[(size_t)v * Q + q] = round + 1;
+            a.value[(size_t)q * V + v] = round + 1;
             want[t] = true;
           }
         } else {
           const int cand = du + __ldg(a.weightsOut + eb + j);
-          const int old = atomicMin(a.value + (size_t)v * Q + q, cand);
+          const int old = atomicMin(a.value + (size_t)q * V + v, cand);
           if (cand < old) {
-            const unsigned o2 = atomicOr(nxt + (size_t)v * W + wq, bit);
+            const unsigned o2 = atomicOr(nxt + (size_t)wq * V + v, bit);
             want[t] = !(o2 & bit);
             if (bk.bound && cand < bk.bound[q] && !(bk.near[wq] & bit)) atomicOr(bk.near + wq, bit);
           }
@@ -618,9 +622,10 @@ static __global__ void batch_init_kernel(int kind, int32_t nVertices, int32_t Q,
 
 // Sources: value 0, their query bit, and the first list (each source
 // vertex once; inList was reset to -1).
-// With a pair list (pairs0 non-null) the first list is (s_q, q) per query.
+// With a pair list (pairs0 non-null) the first list is (s_q, q) per query,
+// and the state is query-major (value[q][v], mask and seen words [w][v]).
 static __global__ void batch_sources_kernel(int kind, int32_t nQueries, int32_t Q, int32_t W,
-                                            const int32_t *sources, int32_t *value,
+                                            int32_t nVertices, const int32_t *sources, int32_t *value,
                                             unsigned *mask0, unsigned *seen,
                                             const int32_t *outOffsets, int32_t *inList,
                                             int32_t *list0, int32_t *list0C,
@@ -629,9 +634,15 @@ static __global__ void batch_sources_kernel(int kind, int32_t nQueries, int32_t 
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nQueries) return;
   const int s = sources[q];
-  value[(size_t)s * Q + q] = 0;
-  atomicOr(mask0 + (size_t)s * W + q / 32, 1u << (q % 32));
-  if (kind == kBatchBFS) atomicOr(seen + (size_t)s * W + q / 32, 1u << (q % 32));
+  if (pairs0) {  // pair batches keep their state query-major
+    value[(size_t)q * nVertices + s] = 0;
+    atomicOr(mask0 + (size_t)(q / 32) * nVertices + s, 1u << (q % 32));
+    if (kind == kBatchBFS) atomicOr(seen + (size_t)(q / 32) * nVertices + s, 1u << (q % 32));
+  } else {
+    value[(size_t)s * Q + q] = 0;
+    atomicOr(mask0 + (size_t)s * W + q / 32, 1u << (q % 32));
+    if (kind == kBatchBFS) atomicOr(seen + (size_t)s * W + q / 32, 1u << (q % 32));
+  }
   if (pairs0) {
     const unsigned long long pos = atomicAdd(listCnt0, 1ull << 32) >> 32;
     pairs0[pos] = (uint32_t)s * (uint32_t)Q + (uint32_t)q;

@@ -303,7 +303,7 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
                                                                      b->bucketMem, b->delta);
   CtlView cv = ctl_view(b);
   gas::detail::batch_sources_kernel<<<(nQ + 127) / 128, 128, 0, b->stream>>>(
-      kind, nQ, Q, W, b->srcDev, b->value, b->mask[0], b->seen, g.outOff, b->inList,
+      kind, nQ, Q, W, g.nV, b->srcDev, b->value, b->mask[0], b->seen, g.outOff, b->inList,
       b->list[0], b->listC[0], cv.listCnt, pairs ? b->pairs[0] : nullptr);
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "batch init");
@@ -316,6 +316,11 @@ gas_status enqueue_batch(gas_batch *b, const CoreGraph &g, int kind, int32_t nQ,
     default: st = launch_run_kind<8>(b, g, kind, Q, blocks, pairs); break;
   }
   if (st) return st;
+  if (pairs) {  // query-major already: the first nQ rows are the results
+    e = cudaMemcpyAsync(b->outDev, b->value, sizeof(int32_t) * (size_t)nQ * g.nV,
+                        cudaMemcpyDeviceToDevice, b->stream);
+    return e == cudaSuccess ? GAS_OK : cuda_fail(e, "batch results");
+  }
   dim3 tb(32, 8), tg((g.nV + 31) / 32, (Q + 31) / 32);
   gas::detail::batch_transpose_kernel<<<tg, tb, 0, b->stream>>>(b->value, g.nV, Q, nQ, b->outDev);
   e = cudaGetLastError();

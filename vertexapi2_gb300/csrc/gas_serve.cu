@@ -405,7 +405,9 @@ void Server::issue_chunk(int l, int rounds, bool final) {
     const int32_t *val = b.kind == 2 ? reinterpret_cast<const int32_t *>(b.pa.rank[kPprRounds & 1])
                                      : b.ba.value;
     dim3 tb(32, 8), tg((V + 31) / 32, (b.Q + 31) / 32);
-    if (V > 0) {
+    if (V > 0 && b.kind != 2 && b.pairs) {  // query-major already: copy the first nQ rows
+      cudaMemcpyAsync(b.out, val, (size_t)b.nQ * V * 4, cudaMemcpyDeviceToDevice, b.stream);
+    } else if (V > 0) {
       gas::detail::batch_transpose_kernel<<<tg, tb, 0, b.stream>>>(val, V, b.Q, b.nQ, b.out);
       launches += 1;
     }
@@ -539,7 +541,7 @@ gas_status Server::launch(int l, const std::shared_ptr<Batch> &bp) {
     gas::detail::batch_init_kernel<<<4 * sms, 256, 0, b.stream>>>(kb, V, b.Q, a.value,
                                                                     a.thresh[0], a.delta);
     gas::detail::batch_sources_kernel<<<(b.nQ + 127) / 128, 128, 0, b.stream>>>(
-        kb, b.nQ, b.Q, b.W, b.sources, a.value, a.mask[0], a.seen, g.bg.g.outOff, a.inList,
+        kb, b.nQ, b.Q, b.W, V, b.sources, a.value, a.mask[0], a.seen, g.bg.g.outOff, a.inList,
         a.list[0], a.listC[0], a.listCnt, b.pairs ? a.pairs[0] : nullptr);
   }
   launches += 2;  // init + sources
