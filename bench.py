@@ -71,13 +71,13 @@ PROGRAM_NAMES = {1: "bfs", 2: "sssp", 3: "cc", 4: "pagerank", 5: "ppr"}
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per run (the
 # run's kernels) from ncu captures of the same command (profiles/): the
-# lattice run's main kernel directly (its one-round dense kernel is 0.15 %
-# of the time and not counted); PageRank's two kernels on R-MAT-20 (3.943
-# GB per run, 16.09 M edges) scaled by edges, its traffic being per-edge
-# gathers and the CSC stream.  None where no capture exists.
+# lattice run's main kernel directly (73.5 + 6.8 MB; its one-round dense
+# kernel is 0.2 % of the time and not counted); PageRank's two kernels on
+# R-MAT-20 (2.381 GB per run, 16.09 M edges) scaled by edges, its traffic
+# being per-edge gathers and the CSC stream.  None where no capture exists.
 TRAFFIC_PER_LAUNCH = {
-    "sssp-grid1024": 84.358144e6 + 17.835520e6,
-    "pagerank-rmat22": (2.757832e9 + 0.411875e9 + 0.672337e9 + 0.101243e9) * (65244320 / 16086703),
+    "sssp-grid1024": 73.507584e6 + 6.810112e6,
+    "pagerank-rmat22": (2.094825e9 + 0.218918e9 + 0.063529e9 + 0.003429e9) * (65244320 / 16086703),
 }
 
 
