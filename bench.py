@@ -74,10 +74,15 @@ PROGRAM_NAMES = {1: "bfs", 2: "sssp", 3: "cc", 4: "pagerank", 5: "ppr"}
 # lattice run's main kernel directly (73.5 + 6.8 MB; its one-round dense
 # kernel is 0.2 % of the time and not counted); PageRank's two kernels on
 # R-MAT-20 (2.381 GB per run, 16.09 M edges) scaled by edges, its traffic
-# being per-edge gathers and the CSC stream.  None where no capture exists.
+# being per-edge gathers and the CSC stream; CC the same way; BFS on R-MAT-16
+# directly.  None where no capture exists.
 TRAFFIC_PER_LAUNCH = {
     "sssp-grid1024": 73.507584e6 + 6.810112e6,
     "pagerank-rmat22": (2.094825e9 + 0.218918e9 + 0.063529e9 + 0.003429e9) * (65244320 / 16086703),
+    # CC's two kernels on R-MAT-20 symmetric (31,406,204 edges), scaled by edges
+    "cc-rmat22": (424.575488e6 + 15.346176e6 + 37.384960e6 + 0.033024e6) * (128308912 / 31406204),
+    # BFS on R-MAT-16 captured at full size
+    "bfs-rmat16": 8.890368e6,
 }
 
 
