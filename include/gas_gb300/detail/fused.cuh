@@ -257,16 +257,26 @@ struct FusedBitsSmem {
 // reads words b + grid * k, NT at a time; a block scan of their bit counts
 // places the set bits' vertices in shared memory in vertex order per word,
 // and the block's threads take them.  Every thread of the block calls it.
+// The word of bitmap `bits` a thread reads first in fused_bits_round (0
+// past the block's words).
+__device__ __forceinline__ uint32_t fused_first_word(const uint32_t *bits, int nWords) {
+  const int w = (int)blockIdx.x + (int)gridDim.x * (int)threadIdx.x;
+  return w < nWords ? bits[w] : 0u;
+}
+
 template <class P, int NT>
 __device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const ScatterArgs &sa,
                                                  const FusedCtx &f, const uint32_t *bits, int nWords,
-                                                 FusedBitsSmem<NT> &sm, FusedCounts &c) {
+                                                 FusedBitsSmem<NT> &sm, FusedCounts &c,
+                                                 bool haveFirst = false, uint32_t first = 0u) {
   const int G = gridDim.x;
   const int perBlock = (nWords - (int)blockIdx.x + G - 1) / G;  // words this block owns
   for (int k0 = 0; k0 < perBlock; k0 += NT) {  // block-uniform
     const int k = k0 + (int)threadIdx.x;
     const int w = (int)blockIdx.x + G * k;
-    const uint32_t word = k < perBlock ? bits[w] : 0u;
+    // the first word may have been loaded already (fused_first_word, read
+    // together with the previous round's counts)
+    const uint32_t word = (k0 == 0 && haveFirst) ? first : (k < perBlock ? bits[w] : 0u);
     const unsigned long long mine = (unsigned long long)__popc(word);
     unsigned long long excl, total;
     block_exclusive_scan_u64<NT>(mine, excl, total, sm.scan);

@@ -289,6 +289,8 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   int cur = ra.cur, sidx = ra.sidx, vcur = 0;
   bool versioned = false;  // the vertex data lives in the fused cells
   bool frontBits = false;  // this round's active set is front_bits(stamp), not a list
+  bool haveFirst = false;  // firstWord holds this thread's first word of front_bits(stamp)
+  uint32_t firstWord = 0u;
   bool capped = false;     // stopped at maxRounds
   bool rangeMode = a.rangeMode != 0;
   int mode = ra.allActive ? kDense : kList;
@@ -365,12 +367,17 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         }
         FusedCounts fc = {0u, 0u, 0u, 0u};
         if (frontBits)
-          fused_bits_round<P, kGNT>(a, sa, f, front_bits(ra, stamp), ra.bitWords, sm.fb, fc);
+          fused_bits_round<P, kGNT>(a, sa, f, front_bits(ra, stamp), ra.bitWords, sm.fb, fc,
+                                    haveFirst, firstWord);
         else
           fused_list_round<P>(a, sa, f, n, T, fc);
         unsigned long long *cnt = ra.denseCnt + kDenseCntStride * (r % 3);
         fused_flush(fc, cnt);
         if (!grid_barrier(ra.barrier, a.errWord)) break;
+        // the next round's bitmap is complete: its first word of this thread
+        // is loaded together with the counts (two independent round trips
+        // in flight instead of one after the other)
+        firstWord = fused_first_word(front_bits(ra, stamp + 1), ra.bitWords);
         statA = cnt[0];
         statR = cnt[1];
         if ((statA >> 32) == 0) break;  // the bitmap was empty: the run ended before this round
@@ -458,6 +465,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       ra.stats[2 * (size_t)r + 1] = statR;
     }
     ++r;
+    haveFirst = nextBits && !denseNext;  // the next round is fused and reads that bitmap
     mode = denseNext ? kDense : kList;
     allActive = false;
     rangeMode = false;
