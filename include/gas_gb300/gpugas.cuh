@@ -206,14 +206,16 @@ class EngineGPU {
   }
 
   // CTAs per SM of the persistent kernel.  Fused-round graphs (small
-  // degrees, latency-bound rounds) run 2 with 128 registers a thread: a
-  // cheaper grid barrier outweighs the lost occupancy.  Other graphs run 4
-  // with 64 registers: more warps in flight for the pull passes, whose
-  // dependent gathers are L2-latency bound.
-  static constexpr int kFusedBlocksPerSM = 2;
+  // degrees, latency-bound rounds) use the instantiation with 128 registers a
+  // thread and launch 1 CTA per SM: the grid barrier and the wait for the
+  // slowest block are cheaper with fewer blocks, and a block's bitmap words
+  // still fit one pass (lattice SSSP 16.65 -> 16.41 ms per run against 2 CTAs
+  // per SM).  Other graphs run 4 with 64 registers: more warps in flight for
+  // the pull passes, whose dependent gathers are L2-latency bound.
+  static constexpr int kFusedBlocksPerSM = 2;  // the fused instantiation's register budget
   static constexpr int kRunBlocksPerSM = 4;
-  // Fused rounds of an apply-only run (BFS: no gather, small frontiers) use
-  // 1 CTA per SM of the same kernel: the barrier is cheaper still.
+  static constexpr int kFusedGatherBlocksPerSM = 1;
+  // Fused rounds of an apply-only run (BFS: no gather) also use 1 CTA per SM.
   static constexpr int kFusedApplyBlocksPerSM = 1;
   // A run that starts with every vertex active runs its leading dense rounds
   // in run_dense_kernel (40 registers, 6 CTAs per SM), then resumes here.
@@ -259,7 +261,8 @@ class EngineGPU {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, detail::kGNT, 0);
       const int want = self->runBlocksPerSM_ > 0
                            ? self->runBlocksPerSM_
-                           : (!ra->fused ? kRunBlocksPerSM : applyOnly ? kFusedApplyBlocksPerSM : kFusedBlocksPerSM);
+                           : (!ra->fused ? kRunBlocksPerSM
+                                         : applyOnly ? kFusedApplyBlocksPerSM : kFusedGatherBlocksPerSM);
       if (want > 0 && want < per) per = want;
       grid = (coop && per > 0 && sms > 0) ? per * sms : -1;
     }
