@@ -621,14 +621,15 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True, stepwi
     run_bytes = float(gbytes.sum() + sbytes.sum())
     kernel_ms = run_kernel_ms / steps
     achieved = run_bytes / (kernel_ms / 1e3) / 1e9 if kernel_ms > 0 else 0.0
-    # range split + (leading dense-rounds kernel when every vertex starts
-    # active) + persistent run
+    # set_active's range split, run()'s zeroing of its counters and round-0
+    # bitmaps, the leading dense-rounds kernel when every vertex starts
+    # active, the persistent run
     dense_first = (lo, hi) == (0, g.n_vertices)
-    launches_per_step = 1 + (1 if w["gather"] else 0) + (1 if dense_first else 0)
+    launches_per_step = 3 + (1 if dense_first else 0)
     kernel_label = ("run_dense_kernel + run_persistent_kernel" if dense_first
                     else "run_persistent_kernel")
     if stepwise:
-        launches_per_step = 2 * rounds
+        launches_per_step = 1 + 2 * rounds
         kernel_label = "gather_apply_kernel + scatter_activate_kernel (stepwise)"
 
     # CPU baseline (one core, the restatement) and parity with the oracle

@@ -135,6 +135,22 @@ __global__ void ell_rows_kernel(int32_t nV, const int32_t *off, const int32_t *i
   }
 }
 
+// The counters, barrier words and round-0 bitmaps a persistent run starts
+// from, zeroed by one launch instead of one memset each.
+struct ZeroSegments {
+  static constexpr int kMax = 8;
+  uint32_t *ptr[kMax];
+  int32_t words[kMax];
+  int32_t n;
+};
+
+__global__ void zero_segments_kernel(ZeroSegments z) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int s = 0; s < z.n; ++s)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < z.words[s]; i += stride)
+      z.ptr[s][i] = 0u;
+}
+
 struct gas_core_s {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -1066,11 +1082,6 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
     A(cudaMemsetAsync(c->frontBits, 0, sizeof(uint32_t) * 3 * std::max(c->bitWords, 1), c->stream));
     c->stamp = 0;
   }
-  A(cudaMemsetAsync(&c->ctl->dense[0][0], 0, sizeof(c->ctl->dense), c->stream));
-  A(cudaMemsetAsync(c->chunkArrive, 0, sizeof(unsigned) * std::max(c->nChunkVertices, 1), c->stream));
-  A(cudaMemsetAsync(&c->ctl->s[0], 0, sizeof(c->ctl->s), c->stream));
-  A(cudaMemsetAsync(&c->ctl->f[c->cur ^ 1], 0, sizeof(ListCtl), c->stream));
-  A(cudaMemsetAsync(&c->ctl->bar[0], 0, sizeof(c->ctl->bar) + sizeof(int32_t), c->stream));
   if (e != cudaSuccess) return cuda_fail(e, "run setup");
 
   gas_run_args ra;
@@ -1120,14 +1131,31 @@ gas_status gas_core_run_persistent(gas_core *c, int32_t maxIters, int32_t haveGa
     ra.frontBits[k] = c->frontBits ? c->frontBits + (size_t)k * c->bitWords : nullptr;
   }
   ra.bitWords = c->bitWords;
-  // round 0 writes the bitmap of stamp stampBase: clear at launch (each round
-  // clears the one after it)
-  A(cudaMemsetAsync(round_bits(c, ra.stampBase), 0, sizeof(uint32_t) * std::max(c->bitWords, 1),
-                    c->stream));
-  // and a fused round 0 writes the active-set bitmap of stampBase + 1
-  if (c->frontBits)
-    A(cudaMemsetAsync(c->frontBits + (size_t)((unsigned)(ra.stampBase + 1) % 3u) * c->bitWords, 0,
-                      sizeof(uint32_t) * std::max(c->bitWords, 1), c->stream));
+  {
+    // per-run counters, the barrier and rounds words, the bitmap round 0
+    // writes (stamp stampBase; each round clears the one after it) and the
+    // active-set bitmap a fused round 0 writes (stampBase + 1)
+    ZeroSegments z;
+    memset(&z, 0, sizeof(z));
+    auto seg = [&](void *p, size_t bytes) {
+      z.ptr[z.n] = static_cast<uint32_t *>(p);
+      z.words[z.n++] = (int32_t)(bytes / sizeof(uint32_t));
+    };
+    seg(&c->ctl->dense[0][0], sizeof(c->ctl->dense));
+    seg(c->chunkArrive, sizeof(unsigned) * std::max(c->nChunkVertices, 1));
+    seg(&c->ctl->s[0], sizeof(c->ctl->s));
+    seg(&c->ctl->f[c->cur ^ 1], sizeof(ListCtl));
+    seg(&c->ctl->bar[0], sizeof(c->ctl->bar) + sizeof(int32_t));
+    seg(round_bits(c, ra.stampBase), sizeof(uint32_t) * std::max(c->bitWords, 1));
+    if (c->frontBits)
+      seg(c->frontBits + (size_t)((unsigned)(ra.stampBase + 1) % 3u) * c->bitWords,
+          sizeof(uint32_t) * std::max(c->bitWords, 1));
+    const int32_t most = std::max(c->bitWords, std::max(c->nChunkVertices, 64));
+    const int blocks = std::min(c->numSMs > 0 ? c->numSMs : 1, (most + 255) / 256);
+    zero_segments_kernel<<<blocks, 256, 0, c->stream>>>(z);
+    A(cudaGetLastError());
+    if (e != cudaSuccess) return cuda_fail(e, "run setup");
+  }
   ra.binMid = c->binMid;
   ra.binSmall = c->binSmall;
   ra.binTiny = c->binTiny;
