@@ -45,16 +45,18 @@ constexpr unsigned kBarrierSpinLimit = 1u << 25;
 // word's top bit flips exactly when the last block arrives, whichever that
 // is, and the low bits return to their value before the barrier.  A block
 // waits until the top bit differs from the one its own atomic returned: no
-// second atomic on the release path.  Returns false on timeout or when
-// another block reported one.
+// second atomic on the release path.  The arrival is a release at GPU scope
+// and the polling load an acquire: with the block barriers around them they
+// order every thread's writes before the barrier ahead of every thread's
+// reads after it, without a sequentially consistent fence on either side.
+// Returns false on timeout or when another block reported one.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
   __shared__ unsigned s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned ok = 1u;
-    __threadfence();
     const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-    const unsigned old = atomicAdd(bar, add);
+    const unsigned old = atom_add_release(bar, add);
     unsigned spins = 0;
     while (((ld_acquire(bar) ^ old) & 0x80000000u) == 0u) {
       ++spins;
@@ -66,7 +68,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
       }
       __nanosleep(32);
     }
-    __threadfence();
     s_ok = ok;
   }
   __syncthreads();
