@@ -349,7 +349,8 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
       // ---------------- push round: list (or range) frontier, or a bitmap
       bool tpvG = true;
       const int ntG = frontBits ? 0 : gather_tiles(a, n, T, frontMaxDeg, tpvG);
-      // fused rounds launch in the 2-CTA/SM instantiation only (launchRun)
+      // fused rounds run in the instantiations of at most 2 CTAs per SM only
+      // (launchRun launches them at 1)
       if (MinBlocks <= 2 && ra.fused && (frontBits || tpvG || !a.haveGather)) {
         // ---------------- fused round: one phase, one barrier
         FusedCtx f;

@@ -206,13 +206,15 @@ class EngineGPU {
   }
 
   // CTAs per SM of the persistent kernel.  Fused-round graphs (small
-  // degrees, latency-bound rounds) use the instantiation with 128 registers a
-  // thread and launch 1 CTA per SM: the grid barrier and the wait for the
-  // slowest block are cheaper with fewer blocks, and a block's bitmap words
-  // still fit one pass (lattice SSSP 16.65 -> 16.41 ms per run against 2 CTAs
-  // per SM).  Other graphs run 4 with 64 registers: more warps in flight for
-  // the pull passes, whose dependent gathers are L2-latency bound.
-  static constexpr int kFusedBlocksPerSM = 2;  // the fused instantiation's register budget
+  // degrees, latency-bound rounds) launch 1 CTA per SM: the grid barrier and
+  // the wait for the slowest block are cheaper with fewer blocks, and a
+  // block's bitmap words still fit one pass (lattice SSSP 16.65 -> 16.41 ms
+  // per run against 2 CTAs per SM).  Their instantiation is compiled for 1
+  // CTA per SM, so it keeps its state in registers (about 250, where a
+  // 128-register budget spilled about 900 bytes a thread to local memory:
+  // 15.68 -> 14.64 ms).  Other graphs run 4 with 64 registers: more warps in
+  // flight for the pull passes, whose dependent gathers are L2-latency bound.
+  static constexpr int kFusedBlocksPerSM = 1;  // the fused instantiation's register budget
   static constexpr int kRunBlocksPerSM = 4;
   static constexpr int kFusedGatherBlocksPerSM = 1;
   // Fused rounds of an apply-only run (BFS: no gather) also use 1 CTA per SM.
