@@ -514,11 +514,14 @@ __device__ __forceinline__ void batch_compact(const BatchArgs &a, const unsigned
 }
 
 // PAIRS: the instantiation for pair-frontier batches (a.pairMode set),
-// which holds only the pair rounds: its smaller register budget (at most 64
+// which holds only the pair rounds: its smaller register budget (at most 40
 // a thread) keeps more warps, and so more of the latency-bound atomics, in
-// flight.  The other instantiation serves vertex-mask batches.
+// flight.  The other instantiation serves vertex-mask batches, at most 64
+// registers a thread so that 4 CTAs fit an SM: its pull and push rounds are
+// latency-bound too (256 R-MAT-21 SSSP queries: 118 ms at 4 CTAs/SM, 170 ms
+// at the 2 a 128-register build allows).
 template <int W, int KIND, bool PAIRS = false>
-__global__ void __launch_bounds__(256, PAIRS ? 6 : 1) batch_run_kernel(const BatchArgs a) {
+__global__ void __launch_bounds__(256, PAIRS ? 6 : 4) batch_run_kernel(const BatchArgs a) {
   __shared__ int32_t sBound[32 * W];
   __shared__ unsigned sNear[W];
   const long long warps = (long long)gridDim.x * (blockDim.x / 32);

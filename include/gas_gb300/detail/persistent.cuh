@@ -45,10 +45,12 @@ constexpr unsigned kBarrierSpinLimit = 1u << 25;
 // word's top bit flips exactly when the last block arrives, whichever that
 // is, and the low bits return to their value before the barrier.  A block
 // waits until the top bit differs from the one its own atomic returned: no
-// second atomic on the release path.  The arrival is a release at GPU scope
-// and the polling load an acquire: with the block barriers around them they
-// order every thread's writes before the barrier ahead of every thread's
-// reads after it, without a sequentially consistent fence on either side.
+// second atomic on the release path.  The block whose atomic flips the bit
+// (the last to arrive) sees that in the value its atomic returned and does
+// not poll.  The arrival is an acquire-release atomic at GPU scope and the
+// polling load an acquire: with the block barriers around them they order
+// every thread's writes before the barrier ahead of every thread's reads
+// after it, without a sequentially consistent fence on either side.
 // Returns false on timeout or when another block reported one.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
   __shared__ unsigned s_ok;
@@ -56,9 +58,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
   if (threadIdx.x == 0) {
     unsigned ok = 1u;
     const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-    const unsigned old = atom_add_release(bar, add);
+    const unsigned old = atom_add_acq_rel(bar, add);
+    const bool last = (((old + add) ^ old) & 0x80000000u) != 0u;
     unsigned spins = 0;
-    while (((ld_acquire(bar) ^ old) & 0x80000000u) == 0u) {
+    while (!last && ((ld_acquire(bar) ^ old) & 0x80000000u) == 0u) {
       ++spins;
       if (spins > kBarrierSpinLimit ||
           ((spins & 4095u) == 0 && (ld_acquire(errWord) & GAS_DEVERR_TIMEOUT))) {

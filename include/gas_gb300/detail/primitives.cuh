@@ -91,9 +91,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-__device__ __forceinline__ unsigned atom_add_release(unsigned *p, unsigned v) {
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned *p, unsigned v) {
   unsigned old;
-  asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
   return old;
 }
 
