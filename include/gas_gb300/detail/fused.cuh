@@ -11,7 +11,7 @@
 // stamp S reads bitmap S % 3, sets bits in bitmap (S + 1) % 3 and clears
 // bitmap (S + 2) % 3 (every round of a run clears one ahead, whatever its
 // kind, so the bitmap a round writes is always clean).  Each block owns the
-// bitmap words b, b + grid, b + 2 * grid, ... (interleaved, so a spatially
+// bitmap bytes b, b + grid, b + 2 * grid, ... (interleaved, so a spatially
 // clustered wavefront spreads over all blocks); it reads them, lists their
 // set bits in shared memory with a block scan, and its threads take the
 // listed vertices.  The first fused round after a list round (or a range)
@@ -245,23 +245,38 @@ __device__ __forceinline__ void fused_list_round(const gas_gather_args &a, const
   }
 }
 
-// Bitmap words a block reads per pass, and the shared-memory list of their
-// set bits (every bit set: 32 vertices a word).
+// The shared-memory list of the vertices a block's threads take in one pass
+// of fused_bits_round (at most 32 a thread), and its scan storage.
 template <int NT>
 struct FusedBitsSmem {
   int32_t vid[NT * 32];
   ScanU64Smem<NT> scan;
 };
 
-// A fused round whose frontier is bitmap `bits` (nWords words): block b
-// reads words b + grid * k, NT at a time; a block scan of their bit counts
-// places the set bits' vertices in shared memory in vertex order per word,
-// and the block's threads take them.  Every thread of the block calls it.
-// The word of bitmap `bits` a thread reads first in fused_bits_round (0
-// past the block's words).
-__device__ __forceinline__ uint32_t fused_first_word(const uint32_t *bits, int nWords) {
-  const int w = (int)blockIdx.x + (int)gridDim.x * (int)threadIdx.x;
-  return w < nWords ? bits[w] : 0u;
+// A fused round whose frontier is bitmap `bits` (nWords words), owned by
+// byte: unit u is bits 8u .. 8u + 7 (vertices 8u .. 8u + 7), and block b
+// owns units b, b + grid, b + 2 * grid, ...  Each thread takes four units a
+// pass (fused_units packs their bytes into one word, so a pass lists at
+// most 32 vertices a thread); a block scan of their bit counts places the
+// set bits' vertices in shared memory, and the block's threads take them.
+// Ownership by byte rather than by 32-bit word spreads a clustered
+// wavefront more evenly: a block's round time grows with its vertex count,
+// and on the 1024x1024 lattice the slowest block's count over the mean,
+// weighted by round size, falls from 1.22 (words) to 1.06 (bytes).  Every
+// thread of the block calls it.
+//
+// The units this thread takes in the pass that starts at k0, packed (byte q
+// = unit blockIdx.x + grid * (k0 + threadIdx.x + NT * q)); 0 past nUnits.
+template <int NT>
+__device__ __forceinline__ uint32_t fused_units(const uint32_t *bits, int nUnits, int k0) {
+  const long long G = gridDim.x;
+  uint32_t packed = 0u;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const long long u = (long long)blockIdx.x + G * (k0 + (int)threadIdx.x + NT * q);
+    if (u < nUnits) packed |= ((bits[u >> 2] >> (8 * (int)(u & 3))) & 0xffu) << (8 * q);
+  }
+  return packed;
 }
 
 template <class P, int NT>
@@ -270,23 +285,23 @@ __device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const
                                                  FusedBitsSmem<NT> &sm, FusedCounts &c,
                                                  bool haveFirst = false, uint32_t first = 0u) {
   const int G = gridDim.x;
-  const int perBlock = (nWords - (int)blockIdx.x + G - 1) / G;  // words this block owns
-  for (int k0 = 0; k0 < perBlock; k0 += NT) {  // block-uniform
-    const int k = k0 + (int)threadIdx.x;
-    const int w = (int)blockIdx.x + G * k;
-    // the first word may have been loaded already (fused_first_word, read
-    // together with the previous round's counts)
-    const uint32_t word = (k0 == 0 && haveFirst) ? first : (k < perBlock ? bits[w] : 0u);
-    const unsigned long long mine = (unsigned long long)__popc(word);
+  const int nUnits = nWords * 4;
+  const int perBlock = (nUnits - (int)blockIdx.x + G - 1) / G;  // units this block owns
+  for (int k0 = 0; k0 < perBlock; k0 += 4 * NT) {  // block-uniform
+    // the first pass's units may have been loaded already (read together
+    // with the previous round's counts)
+    const uint32_t packed = (k0 == 0 && haveFirst) ? first : fused_units<NT>(bits, nUnits, k0);
+    const unsigned long long mine = (unsigned long long)__popc(packed);
     unsigned long long excl, total;
     block_exclusive_scan_u64<NT>(mine, excl, total, sm.scan);
     if (total == 0ull) continue;  // block-uniform (the scan ends with a barrier)
     int off = (int)excl;
-    uint32_t rest = word;
+    uint32_t rest = packed;
     while (rest) {
-      const int b = __ffs(rest) - 1;
+      const int p = __ffs(rest) - 1;
       rest &= rest - 1u;
-      sm.vid[off++] = w * 32 + b;
+      const int u = (int)blockIdx.x + G * (k0 + (int)threadIdx.x + NT * (p >> 3));
+      sm.vid[off++] = u * 8 + (p & 7);
     }
     __syncthreads();
     if (f.width == 4) {  // two listed vertices a thread, their loads interleaved

@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
   int cur = ra.cur, sidx = ra.sidx, vcur = 0;
   bool versioned = false;  // the vertex data lives in the fused cells
   bool frontBits = false;  // this round's active set is front_bits(stamp), not a list
-  bool haveFirst = false;  // firstWord holds this thread's first word of front_bits(stamp)
+  bool haveFirst = false;  // firstWord holds this thread's first-pass bytes of front_bits(stamp)
   uint32_t firstWord = 0u;
   bool capped = false;     // stopped at maxRounds
   bool rangeMode = a.rangeMode != 0;
@@ -379,10 +379,10 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         unsigned long long *cnt = ra.denseCnt + kDenseCntStride * (r % 3);
         fused_flush(fc, cnt);
         if (!grid_barrier(ra.barrier, a.errWord)) break;
-        // the next round's bitmap is complete: its first word of this thread
-        // is loaded together with the counts (two independent round trips
-        // in flight instead of one after the other)
-        firstWord = fused_first_word(front_bits(ra, stamp + 1), ra.bitWords);
+        // the next round's bitmap is complete: this thread's first-pass
+        // bytes of it are loaded together with the counts (independent round
+        // trips in flight instead of one after the other)
+        firstWord = fused_units<kGNT>(front_bits(ra, stamp + 1), ra.bitWords * 4, 0);
         statA = cnt[0];
         statR = cnt[1];
         if ((statA >> 32) == 0) break;  // the bitmap was empty: the run ended before this round
