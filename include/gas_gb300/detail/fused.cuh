@@ -77,6 +77,57 @@ __device__ __forceinline__ FusedCell<VD> load_cell(const FusedCell<VD> *p) {
   return u.c;
 }
 
+// A whole cell in one store per 16 bytes: the writer's slot and version
+// change, the other slot is rewritten with the value it already holds, so a
+// reader that sees any mix of the old and new words still takes the right
+// value (it reads the unchanged slot unless the version it sees is older
+// than this round, and then the slot that version names, also unchanged).
+template <class VD>
+__device__ __forceinline__ void store_cell(FusedCell<VD> *p, const FusedCell<VD> &c) {
+  constexpr int N = (int)(sizeof(FusedCell<VD>) / 16);
+  union {
+    int4 w[N];
+    FusedCell<VD> c;
+  } u;
+  u.c = c;
+#pragma unroll
+  for (int k = 0; k < N; ++k) reinterpret_cast<int4 *>(p)[k] = u.w[k];
+}
+
+// Sets the bits of out-neighbours out[0..W) (-1: none) in `bits`, one
+// atomic per distinct bitmap word (a lattice vertex's left and right
+// neighbours usually share one).  Returns the number of out-neighbours.
+template <int W>
+__device__ __forceinline__ unsigned set_out_bits(uint32_t *bits, const int32_t (&out)[W]) {
+  unsigned n = 0u;
+  if constexpr (W <= 4) {
+    uint32_t mask[W];
+#pragma unroll
+    for (int j = 0; j < W; ++j) mask[j] = out[j] >= 0 ? 1u << (out[j] & 31) : 0u;
+#pragma unroll
+    for (int j = 1; j < W; ++j)
+#pragma unroll
+      for (int i = 0; i < j; ++i)
+        if (mask[i] && mask[j] && (out[i] >> 5) == (out[j] >> 5)) {
+          mask[i] |= mask[j];
+          mask[j] = 0u;
+        }
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      n += out[j] >= 0 ? 1u : 0u;
+      if (mask[j]) atomicOr(bits + (out[j] >> 5), mask[j]);  // result unused: a reduction
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+      if (out[j] >= 0) {
+        bit_set(bits, out[j]);
+        ++n;
+      }
+  }
+  return n;
+}
+
 // v's value as of the end of the previous round.
 template <class VD>
 __device__ __forceinline__ VD fused_read(const FusedCtx &f, int v) {
@@ -180,19 +231,18 @@ __device__ __forceinline__ void fused_vertices(const gas_gather_args &a, const F
           ++deg;
         }
       const bool r = do_apply<P>(&t, acc, a.iteration);
-      FusedCell<VD> *cell = reinterpret_cast<FusedCell<VD> *>(f.cells) + vs[k];
-      cell->s[own ^ 1] = t;
-      cell->ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
+      FusedCell<VD> nc = cv[k];
+      if (own)
+        nc.s[0] = t;
+      else
+        nc.s[1] = t;
+      nc.ver = (f.stamp << 1) | (uint32_t)(own ^ 1);
+      store_cell(reinterpret_cast<FusedCell<VD> *>(f.cells) + vs[k], nc);
       ++c.active;
       c.inEdges += deg;
       if (r) {
         ++c.ret;
-#pragma unroll
-        for (int j = 0; j < W; ++j)
-          if (outd[k][j] >= 0) {
-            bit_set(f.nextBits, outd[k][j]);
-            ++c.outEdges;
-          }
+        c.outEdges += set_out_bits<W>(f.nextBits, outd[k]);
       }
     }
   } else {  // apply only: nothing reads other vertices, update in place
@@ -206,12 +256,7 @@ __device__ __forceinline__ void fused_vertices(const gas_gather_args &a, const F
       c.inEdges += (unsigned)(a.inOffsets[vs[k] + 1] - a.inOffsets[vs[k]]);
       if (r) {
         ++c.ret;
-#pragma unroll
-        for (int j = 0; j < W; ++j)
-          if (outd[k][j] >= 0) {
-            bit_set(f.nextBits, outd[k][j]);
-            ++c.outEdges;
-          }
+        c.outEdges += set_out_bits<W>(f.nextBits, outd[k]);
       }
     }
   }
