@@ -11,8 +11,8 @@
 // stamp S reads bitmap S % 3, sets bits in bitmap (S + 1) % 3 and clears
 // bitmap (S + 2) % 3 (every round of a run clears one ahead, whatever its
 // kind, so the bitmap a round writes is always clean).  Each block owns the
-// bitmap bytes b, b + grid, b + 2 * grid, ... (interleaved, so a spatially
-// clustered wavefront spreads over all blocks); it reads them, lists their
+// bitmap byte slots b, b + grid, b + 2 * grid, ... (interleaved, so a
+// spatially clustered wavefront spreads over all blocks); it reads them, lists their
 // set bits in shared memory with a block scan, and its threads take the
 // listed vertices.  The first fused round after a list round (or a range)
 // reads that list instead, dealing its entries across all blocks.  Round
@@ -299,27 +299,34 @@ struct FusedBitsSmem {
 };
 
 // A fused round whose frontier is bitmap `bits` (nWords words), owned by
-// byte: unit u is bits 8u .. 8u + 7 (vertices 8u .. 8u + 7), and block b
-// owns units b, b + grid, b + 2 * grid, ...  Each thread takes four units a
-// pass (fused_units packs their bytes into one word, so a pass lists at
-// most 32 vertices a thread); a block scan of their bit counts places the
-// set bits' vertices in shared memory, and the block's threads take them.
-// Ownership by byte rather than by 32-bit word spreads a clustered
-// wavefront more evenly: a block's round time grows with its vertex count,
-// and on the 1024x1024 lattice the slowest block's count over the mean,
-// weighted by round size, falls from 1.22 (words) to 1.06 (bytes).  Every
-// thread of the block calls it.
+// slot: slot s is byte lane s & 3 of the 32 consecutive words of group
+// s >> 2 (vertices 1024 g + 32 i + 8 j .. + 7 for word i of the group), and
+// block b owns slots b, b + grid, b + 2 * grid, ...  A warp takes four slots
+// a pass, a lane one word of each (32 consecutive words: one coalesced
+// load), so a thread's four bytes pack into one word and a pass lists at
+// most 32 vertices a thread; a block scan of their bit counts places the set
+// bits' vertices in shared memory, and the block's threads take them.
+// Owning bytes rather than 32-bit words spreads a clustered wavefront more
+// evenly: a block's round time grows with its vertex count, and on the
+// 1024x1024 lattice the slowest block's count over the mean, weighted by
+// round size, falls from 1.22 (words) to 1.10 (this layout; 1.06 for bytes
+// dealt one by one, whose loads do not coalesce).  Every thread of the block
+// calls it.
 //
-// The units this thread takes in the pass that starts at k0, packed (byte q
-// = unit blockIdx.x + grid * (k0 + threadIdx.x + NT * q)); 0 past nUnits.
+// The slots' bytes this thread takes in the pass that starts at k0, packed
+// (byte q: slot blockIdx.x + grid * (k0 + 4 * warp + q), word lane of its
+// group); 0 past the bitmap.
 template <int NT>
-__device__ __forceinline__ uint32_t fused_units(const uint32_t *bits, int nUnits, int k0) {
+__device__ __forceinline__ uint32_t fused_units(const uint32_t *bits, int nWords, int k0) {
   const long long G = gridDim.x;
+  const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+  const long long nSlots = 4ll * ((nWords + 31) / 32);
   uint32_t packed = 0u;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    const long long u = (long long)blockIdx.x + G * (k0 + (int)threadIdx.x + NT * q);
-    if (u < nUnits) packed |= ((bits[u >> 2] >> (8 * (int)(u & 3))) & 0xffu) << (8 * q);
+    const long long s = (long long)blockIdx.x + G * (k0 + 4 * warp + q);
+    const long long w = 32 * (s >> 2) + lane;
+    if (s < nSlots && w < nWords) packed |= ((bits[w] >> (8 * (int)(s & 3))) & 0xffu) << (8 * q);
   }
   return packed;
 }
@@ -330,12 +337,13 @@ __device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const
                                                  FusedBitsSmem<NT> &sm, FusedCounts &c,
                                                  bool haveFirst = false, uint32_t first = 0u) {
   const int G = gridDim.x;
-  const int nUnits = nWords * 4;
-  const int perBlock = (nUnits - (int)blockIdx.x + G - 1) / G;  // units this block owns
-  for (int k0 = 0; k0 < perBlock; k0 += 4 * NT) {  // block-uniform
+  const int nSlots = 4 * ((nWords + 31) / 32);
+  const int perBlock = (nSlots - (int)blockIdx.x + G - 1) / G;  // slots this block owns
+  const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+  for (int k0 = 0; k0 < perBlock; k0 += 4 * (NT / 32)) {  // block-uniform
     // the first pass's units may have been loaded already (read together
     // with the previous round's counts)
-    const uint32_t packed = (k0 == 0 && haveFirst) ? first : fused_units<NT>(bits, nUnits, k0);
+    const uint32_t packed = (k0 == 0 && haveFirst) ? first : fused_units<NT>(bits, nWords, k0);
     const unsigned long long mine = (unsigned long long)__popc(packed);
     unsigned long long excl, total;
     block_exclusive_scan_u64<NT>(mine, excl, total, sm.scan);
@@ -345,8 +353,8 @@ __device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const
     while (rest) {
       const int p = __ffs(rest) - 1;
       rest &= rest - 1u;
-      const int u = (int)blockIdx.x + G * (k0 + (int)threadIdx.x + NT * (p >> 3));
-      sm.vid[off++] = u * 8 + (p & 7);
+      const int sl = (int)blockIdx.x + G * (k0 + 4 * warp + (p >> 3));
+      sm.vid[off++] = 32 * (32 * (sl >> 2) + lane) + 8 * (sl & 3) + (p & 7);
     }
     __syncthreads();
     if (f.width == 4) {  // two listed vertices a thread, their loads interleaved

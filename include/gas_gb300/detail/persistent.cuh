@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         // the next round's bitmap is complete: this thread's first-pass
         // bytes of it are loaded together with the counts (independent round
         // trips in flight instead of one after the other)
-        firstWord = fused_units<kGNT>(front_bits(ra, stamp + 1), ra.bitWords * 4, 0);
+        firstWord = fused_units<kGNT>(front_bits(ra, stamp + 1), ra.bitWords, 0);
         statA = cnt[0];
         statR = cnt[1];
         if ((statA >> 32) == 0) break;  // the bitmap was empty: the run ended before this round
