@@ -369,31 +369,6 @@ __device__ __forceinline__ void fused_bits_round(const gas_gather_args &a, const
   }
 }
 
-// Adds the block's fused-round counts into cnt[0] = (active << 32 |
-// in-edges) and cnt[1] = (returned << 32 | out-edges): one atomic each per
-// block.  Every thread of the block calls it.
-__device__ __forceinline__ void fused_flush(const FusedCounts &c, unsigned long long *cnt) {
-  __shared__ unsigned long long sA[32], sR[32];
-  const unsigned wA = __reduce_add_sync(kFullMask, c.active);
-  const unsigned wEin = __reduce_add_sync(kFullMask, c.inEdges);
-  const unsigned wR = __reduce_add_sync(kFullMask, c.ret);
-  const unsigned wEout = __reduce_add_sync(kFullMask, c.outEdges);
-  if ((threadIdx.x & 31) == 0) {
-    sA[threadIdx.x >> 5] = ((unsigned long long)wA << 32) | wEin;
-    sR[threadIdx.x >> 5] = ((unsigned long long)wR << 32) | wEout;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned long long x = 0ull, y = 0ull;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      x += sA[k];
-      y += sR[k];
-    }
-    if (x) atomicAdd(cnt, x);
-    if (y) atomicAdd(cnt + 1, y);
-  }
-}
-
 // A frontier left in bitmap `bits` becomes the list `out` (in-degree
 // prefix, CSC begin, the gather's tile splits and maximum degree), in
 // vertex order per block: for a run that stops at maxRounds after a fused

@@ -52,26 +52,61 @@ constexpr unsigned kBarrierSpinLimit = 1u << 25;
 // every thread's writes before the barrier ahead of every thread's reads
 // after it, without a sequentially consistent fence on either side.
 // Returns false on timeout or when another block reported one.
+//
+// barrier_thread0 is thread 0's part, between the block barriers.
+__device__ __forceinline__ bool barrier_thread0(unsigned *bar, unsigned *errWord) {
+  const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+  const unsigned old = atom_add_acq_rel(bar, add);
+  if ((((old + add) ^ old) & 0x80000000u) != 0u) return true;  // the last arrival
+  unsigned spins = 0;
+  while (((ld_acquire(bar) ^ old) & 0x80000000u) == 0u) {
+    ++spins;
+    if (spins > kBarrierSpinLimit ||
+        ((spins & 4095u) == 0 && (ld_acquire(errWord) & GAS_DEVERR_TIMEOUT))) {
+      atomicOr(errWord, GAS_DEVERR_TIMEOUT);
+      return false;
+    }
+    __nanosleep(32);
+  }
+  return true;
+}
+
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned *errWord) {
   __shared__ unsigned s_ok;
   __syncthreads();
+  if (threadIdx.x == 0) s_ok = barrier_thread0(bar, errWord) ? 1u : 0u;
+  __syncthreads();
+  return s_ok != 0u;
+}
+
+// The grid barrier that closes a fused round, with the round's counts: the
+// warps' sums meet in shared memory at the barrier's first block barrier,
+// and thread 0 adds the block's totals into cnt[0] (active << 32 |
+// in-edges) and cnt[1] (ret << 32 | out-edges) just before it arrives (one
+// block barrier instead of one for the counts and one for the grid
+// barrier).  Every thread of the block calls it with its own counts.
+__device__ __forceinline__ bool fused_barrier(unsigned *bar, unsigned *errWord, const FusedCounts &c,
+                                              unsigned long long *cnt) {
+  __shared__ unsigned long long sA[32], sR[32];
+  __shared__ unsigned s_ok;
+  const unsigned wA = __reduce_add_sync(kFullMask, c.active);
+  const unsigned wEin = __reduce_add_sync(kFullMask, c.inEdges);
+  const unsigned wR = __reduce_add_sync(kFullMask, c.ret);
+  const unsigned wEout = __reduce_add_sync(kFullMask, c.outEdges);
+  if ((threadIdx.x & 31) == 0) {
+    sA[threadIdx.x >> 5] = ((unsigned long long)wA << 32) | wEin;
+    sR[threadIdx.x >> 5] = ((unsigned long long)wR << 32) | wEout;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned ok = 1u;
-    const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-    const unsigned old = atom_add_acq_rel(bar, add);
-    const bool last = (((old + add) ^ old) & 0x80000000u) != 0u;
-    unsigned spins = 0;
-    while (!last && ((ld_acquire(bar) ^ old) & 0x80000000u) == 0u) {
-      ++spins;
-      if (spins > kBarrierSpinLimit ||
-          ((spins & 4095u) == 0 && (ld_acquire(errWord) & GAS_DEVERR_TIMEOUT))) {
-        atomicOr(errWord, GAS_DEVERR_TIMEOUT);
-        ok = 0u;
-        break;
-      }
-      __nanosleep(32);
+    unsigned long long x = 0ull, y = 0ull;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      x += sA[k];
+      y += sR[k];
     }
-    s_ok = ok;
+    if (x) atomicAdd(cnt, x);
+    if (y) atomicAdd(cnt + 1, y);
+    s_ok = barrier_thread0(bar, errWord) ? 1u : 0u;
   }
   __syncthreads();
   return s_ok != 0u;
@@ -377,8 +412,7 @@ __global__ void __launch_bounds__(kGNT, MinBlocks) run_persistent_kernel(const g
         else
           fused_list_round<P>(a, sa, f, n, T, fc);
         unsigned long long *cnt = ra.denseCnt + kDenseCntStride * (r % 3);
-        fused_flush(fc, cnt);
-        if (!grid_barrier(ra.barrier, a.errWord)) break;
+        if (!fused_barrier(ra.barrier, a.errWord, fc, cnt)) break;
         // the next round's bitmap is complete: this thread's first-pass
         // bytes of it are loaded together with the counts (independent round
         // trips in flight instead of one after the other)
