@@ -71,13 +71,13 @@ PROGRAM_NAMES = {1: "bfs", 2: "sssp", 3: "cc", 4: "pagerank", 5: "ppr"}
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per run (the
 # run's kernels) from ncu captures of the same command (profiles/): the
-# lattice run's two kernels directly (main kernel 71.7 + 5.2 MB, one-round
-# dense kernel 41.1 + 0.3 MB, L2 flushed before the step); PageRank's two kernels on
+# lattice run's two kernels directly (main kernel 71.7 + 4.0 MB, one-round
+# dense kernel 41.1 + 0.4 MB, L2 flushed before the step); PageRank's two kernels on
 # R-MAT-20 (2.381 GB per run, 16.09 M edges) scaled by edges, its traffic
 # being per-edge gathers and the CSC stream; CC the same way; BFS on R-MAT-16
 # directly.  None where no capture exists.
 TRAFFIC_PER_LAUNCH = {
-    "sssp-grid1024": 71.708416e6 + 5.248256e6 + 41.136896e6 + 0.315392e6,
+    "sssp-grid1024": 71.680512e6 + 4.024320e6 + 41.136896e6 + 0.366080e6,
     "pagerank-rmat22": (2.094825e9 + 0.218918e9 + 0.063529e9 + 0.003429e9) * (65244320 / 16086703),
     # CC's two kernels on R-MAT-20 symmetric (31,406,204 edges), scaled by edges
     "cc-rmat22": (424.575488e6 + 15.346176e6 + 37.384960e6 + 0.033024e6) * (128308912 / 31406204),
