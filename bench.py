@@ -616,6 +616,17 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True, stepwi
     eng.close()
     del flush
     nbytes = init.nbytes
+    # per-step device times (min and median of the timed steps), and for BFS
+    # the Graph500 count: edges within the reached component / 2 per second
+    step_stats = {"min": float(np.min(step_ms)), "median": float(np.median(step_ms)),
+                  "n": len(step_ms)}
+    graph500 = None
+    if w["program"] == 1:
+        reached = init != -1
+        outdeg = np.bincount(g.srcs, minlength=g.n_vertices)
+        comp_edges = float(outdeg[reached].sum()) / 2.0
+        graph500 = {"gteps": comp_edges / (step_stats["median"] / 1e3) / 1e9,
+                    "edges_in_component": comp_edges, "at": "median step"}
 
     peak, peak_kind = measured_peak()
     run_bytes = float(gbytes.sum() + sbytes.sum())
@@ -670,7 +681,8 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True, stepwi
         "run": {"rounds": rounds, "edges_traversed_per_run": edges_per_run,
                 "driver": "stepwise (host loop per round)" if stepwise else "run() (persistent)",
                 "l2": "flushed before every timed step, device-timed and end-to-end (512 MB write)",
-                "parallelism": f"replicas x{world}", "set_graph_ms": set_graph_ms},
+                "parallelism": f"replicas x{world}", "set_graph_ms": set_graph_ms,
+                "step_ms": step_stats},
         "roofline": {"bound": "hbm", "kernel": kernel_label, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind,
@@ -689,6 +701,7 @@ def measure_plain(name, steps, warmup, world, rank, local, with_cpu=True, stepwi
         "gpu_launches": launches_per_step * steps,
         "clocks": clk.summary(),
         "wall_s_timed": wall,
+        **({"graph500": graph500} if graph500 else {}),
     }
 
 
