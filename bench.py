@@ -1133,7 +1133,7 @@ def per_algo_entry(line: dict) -> dict:
     """The per_algo summary of a workload's line."""
     keep = ("value", "unit", "steps", "warmup", "ms_per_step", "dtype", "config", "run", "roofline",
             "cpu_baseline", "parity", "e2e", "gpu_launches", "clocks", "one_at_a_time", "per_set",
-            "latency_ms", "sweep", "mean_batch", "plain_ms", "alone_served_ms", "server")
+            "latency_ms", "sweep", "mean_batch", "plain_ms", "alone_served_ms", "server", "graph500")
     return {k: line[k] for k in keep if k in line}
 
 
