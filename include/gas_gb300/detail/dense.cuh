@@ -365,30 +365,8 @@ __device__ void dense_warp_unit(const DenseCtx &a, long long u, DenseCounts &c) 
     const int beg = a.inOffsets[v], end = mark_inactive(a, v) ? beg : a.inOffsets[v + 1];
     typedef typename P::VertexData VD;
     const VD *vd = reinterpret_cast<const VD *>(a.vdCur);
-    // the (at most three) 16-byte quads of source ids covering [beg, end);
-    // the edge arrays are padded to whole quads
-    static_assert(GAS_TPV_MAX_DEGREE == 8, "three quads cover 8 edges at any alignment");
-    int w[12];
-    const int q0 = beg >> 2, nq = end > beg ? ((end - 1) >> 2) - q0 + 1 : 0;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      int4 t = make_int4(0, 0, 0, 0);
-      if (k < nq) t = __ldg(reinterpret_cast<const int4 *>(a.inSources) + q0 + k);
-      w[4 * k] = t.x;
-      w[4 * k + 1] = t.y;
-      w[4 * k + 2] = t.z;
-      w[4 * k + 3] = t.w;
-    }
-    const int off = beg & 3;
     int src[GAS_TPV_MAX_DEGREE];
-#pragma unroll
-    for (int k = 0; k < GAS_TPV_MAX_DEGREE; ++k) {
-      int x0 = w[k];
-      x0 = off == 1 ? w[k + 1] : x0;
-      x0 = off == 2 ? w[k + 2] : x0;
-      x0 = off == 3 ? w[k + 3] : x0;
-      src[k] = x0;
-    }
+    load_window8(a.inSources, beg, end, src);
     GR g = gz;
     unsigned act = 0u;
 #pragma unroll

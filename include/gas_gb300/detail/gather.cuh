@@ -383,14 +383,27 @@ __device__ void tpv_gather_tile(const gas_gather_args &a, int t, int n, int T,
     front_entry(a, i, n, T, v, pre, end, beg);
     const int deg = end - pre;
     const int obeg = a.outOffsets[v], oend = a.outOffsets[v + 1];
-    int src[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) src[k] = k < deg ? __ldg(a.inSources + beg + k) : 0;
+    // source ids (and 4-byte edge data) as 16-byte quads: at most three
+    // each for the <= 8 in-edges at any alignment (the arrays are padded)
+    typedef typename P::EdgeData ED;
+    constexpr bool kQuadEd = !std::is_empty<ED>::value && sizeof(ED) == 4;
+    int src[D], edw[kQuadEd ? D : 1];
+    load_window8(a.inSources, beg, beg + deg, src);
+    if constexpr (kQuadEd) load_window8(static_cast<const int32_t *>(a.edgeData), beg, beg + deg, edw);
     GR acc = P::gatherZero;
 #pragma unroll
     for (int k = 0; k < D; ++k)
-      if (k < deg)
-        acc = P::gatherReduce(acc, P::gatherMap(vd + v, vd + src[k], edge_ptr<P>(a.edgeData, beg + k)));
+      if (k < deg) {
+        const ED *ep;
+        ED e;
+        if constexpr (kQuadEd) {
+          memcpy(&e, &edw[k], sizeof(ED));
+          ep = &e;
+        } else {
+          ep = edge_ptr<P>(a.edgeData, beg + k);
+        }
+        acc = P::gatherReduce(acc, P::gatherMap(vd + v, vd + src[k], ep));
+      }
     VD tmp = vd[v];
     const bool r = do_apply<P>(&tmp, acc, a.iteration);
     vnew[i] = tmp;

@@ -85,6 +85,33 @@ __device__ __forceinline__ T load_cg(const T *p) {
   return r;
 }
 
+// Entries [beg, end) (end - beg <= 8) of an int32 array padded to whole
+// 16-byte quads, as out[0..end-beg): the at most three quads covering them,
+// then a shift by beg % 4 (selects, no local-memory indexing).
+__device__ __forceinline__ void load_window8(const int32_t *arr, int beg, int end, int (&out)[8]) {
+  static_assert(GAS_TPV_MAX_DEGREE == 8, "three quads cover 8 entries at any alignment");
+  int w[12];
+  const int q0 = beg >> 2, nq = end > beg ? ((end - 1) >> 2) - q0 + 1 : 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    int4 t = make_int4(0, 0, 0, 0);
+    if (k < nq) t = __ldg(reinterpret_cast<const int4 *>(arr) + q0 + k);
+    w[4 * k] = t.x;
+    w[4 * k + 1] = t.y;
+    w[4 * k + 2] = t.z;
+    w[4 * k + 3] = t.w;
+  }
+  const int off = beg & 3;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    int x0 = w[k];
+    x0 = off == 1 ? w[k + 1] : x0;
+    x0 = off == 2 ? w[k + 2] : x0;
+    x0 = off == 3 ? w[k + 3] : x0;
+    out[k] = x0;
+  }
+}
+
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
